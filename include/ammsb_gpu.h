@@ -1,0 +1,236 @@
+/*
+ * ammsb_gpu.h -- C ABI of the GB300 a-MMSB SG-MCMC sampler (libammsb_gpu.so).
+ *
+ * The reference has no plugin or FFI surface: its hot path sits behind the
+ * C++ class mcmc::learning::MCMCSamplerStochastic (learner.h:45 run(),
+ * mcmc_sampler_stochastic.h:72-85), constructed from mcmc::Options
+ * (options.h:129-315) and driven by apps/main/main.cc:69-76 as
+ *   MCMCSamplerStochastic s(args); s.init(); s.run();
+ * This header is that boundary as plain C: a handle owns the sampler state
+ * resident in GPU memory; host arrays passed in are borrowed for the call.
+ *
+ * Conventions
+ *   - every function returns AMMSB_OK (0) or a negative AMMSB_E* status;
+ *     ammsb_last_error() gives the message.  No C++ exception crosses the ABI
+ *     (the reference throws MCMCException, exception.h:12-28).
+ *   - a handle is bound to one CUDA device and one stream and is not
+ *     thread-safe, like the reference's single-threaded sequential sampler.
+ *   - vertex ids are int32 (mcmc::Vertex, data.h:42); edges are unordered
+ *     pairs (a, b); sets store a < b as the reference's Edge(min, max).
+ */
+#ifndef AMMSB_GPU_H_
+#define AMMSB_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMMSB_OK 0
+#define AMMSB_E_ARG (-1)       /* invalid argument (InvalidArgumentException) */
+#define AMMSB_E_CUDA (-2)      /* CUDA runtime error */
+#define AMMSB_E_SAMPLING (-3)  /* a capped rejection loop gave up */
+#define AMMSB_E_CAPACITY (-4)  /* minibatch exceeds its buffer (BufferSizeException) */
+#define AMMSB_E_STATE (-5)     /* call order / state error */
+#define AMMSB_E_UNSUPPORTED (-6)
+
+/* mcmc.strategy values, types.h:11-16 */
+#define AMMSB_STRATIFIED_RANDOM_NODE 0
+#define AMMSB_STRATIFIED_RANDOM_NODE_LINKS 1
+#define AMMSB_STRATIFIED_RANDOM_NODE_NONLINKS 2
+#define AMMSB_RANDOM_EDGE 3
+
+/* storage type of pi (GB300 option; the reference stores Float = float) */
+#define AMMSB_PI_F32 0
+#define AMMSB_PI_BF16 1
+
+/* The sampler's option surface, options.h:142-185 (mcmc.* flags).  Zero
+ * values take the reference's derived defaults at ammsb_create():
+ * a := b^-c (options.h:257-259), alpha := 1/K (options.h:260-262),
+ * held_out_ratio := 0.1 (learner.cc:88-92), interval := 50 (seq cc:15-19),
+ * stats_print_interval := 64Ki (cc:20-24), num_node_sample := N/50 and
+ * mini_batch_size := N/10 (cc:35-44). */
+typedef struct ammsb_options {
+  double alpha;                 /* mcmc.alpha, default 0 (=> 1/K) */
+  double eta0;                  /* mcmc.eta0, default 1 */
+  double eta1;                  /* mcmc.eta1, default 1 */
+  double epsilon;               /* mcmc.epsilon, default 1e-7 */
+  double a;                     /* mcmc.a, default 0 (=> b^-c) */
+  double b;                     /* mcmc.b, default 1024 */
+  double c;                     /* mcmc.c, default 0.5 */
+  int64_t K;                    /* mcmc.K, default 300 */
+  int64_t mini_batch_size;      /* mcmc.mini-batch-size, default 0 */
+  int64_t num_node_sample;      /* mcmc.num-node-sample, default 0 */
+  int32_t strategy;             /* mcmc.strategy, default stratified-random-node */
+  int64_t sampler_max_source;   /* mcmc.sampler.max-source, default 1 */
+  int64_t max_iteration;        /* mcmc.max-iteration, default 10000000 */
+  int64_t interval;             /* mcmc.interval, default 0 (=> 50) */
+  int64_t stats_print_interval; /* mcmc.stats, default 0 (=> 65536) */
+  int64_t num_updates;          /* mcmc.num-updates, default 1000 (unused, kept) */
+  double held_out_ratio;        /* mcmc.held-out-ratio, default 0 (=> 0.1) */
+  int32_t random_seed;          /* mcmc.seed, default 42 */
+  double convergence_threshold; /* mcmc.convergence, default 1e-12 */
+  /* GB300 options (no reference counterpart) */
+  int32_t pi_dtype;             /* AMMSB_PI_F32 (default) or AMMSB_PI_BF16 */
+  int32_t chain;                /* Philox key word 1: independent chain id */
+  int32_t device;               /* CUDA device ordinal, default 0 */
+  int32_t use_graph;            /* capture the iteration in a CUDA graph (1) */
+  int32_t verbose;              /* info lines on stderr like learner.cc:105-120 */
+} ammsb_options;
+
+/* Undirected graph as symmetric CSR: row v lists the neighbours of v in
+ * ascending order; row_ptr[n] = 2E.  Replaces NetworkGraph (data.h:135-313). */
+typedef struct ammsb_graph {
+  int64_t n;
+  const int64_t *row_ptr; /* n + 1 */
+  const int32_t *col;     /* row_ptr[n] */
+} ammsb_graph;
+
+/* Held-out or test set: EdgeMap{Edge -> bool is_edge} (data.h:131) as
+ * arrays; a[i] < b[i]; iteration order is array order. */
+typedef struct ammsb_edge_set {
+  int64_t count;
+  const int32_t *a;
+  const int32_t *b;
+  const uint8_t *y;
+} ammsb_edge_set;
+
+typedef struct ammsb_handle ammsb_handle;
+
+/* Fills the reference defaults of options.h:144-185. */
+void ammsb_options_default(ammsb_options *opt);
+
+/* Learner::Learner + Network::Init + Learner::Init + the sampler constructor
+ * (learner.cc:13-84, network.cc:31-84, mcmc_sampler_stochastic.cc:9-44):
+ * validates options, derives defaults, uploads the graph and the held-out
+ * and test sets, allocates the state in GPU memory. */
+int ammsb_create(const ammsb_options *opt, const ammsb_graph *graph,
+                 const ammsb_edge_set *held_out, const ammsb_edge_set *test,
+                 ammsb_handle **out);
+void ammsb_destroy(ammsb_handle *h);
+const char *ammsb_last_error(const ammsb_handle *h);
+/* Message of the last ammsb_create() failure on this thread. */
+const char *ammsb_create_error(void);
+
+/* MCMCSamplerStochastic::init (cc:29-79): theta ~ Gamma(eta0, eta1) (K x 2),
+ * beta = theta[:,1] / sum, phi ~ Gamma(1, 1) (N x K), pi = row-normalised
+ * phi.  Draws follow the Philox streams of ammsb_rng.h. */
+int ammsb_init_state(ammsb_handle *h);
+/* Loads a given state instead: phi N x K float, theta K x 2 double. */
+int ammsb_set_state(ammsb_handle *h, const float *phi, const double *theta);
+
+/* n_iters iterations of the loop body of run() (cc:131-174): minibatch,
+ * neighbour sets, update_phi, pi, update_beta, step_count++.  No
+ * perplexity.  Launched as one CUDA graph per iteration when use_graph. */
+int ammsb_step(ammsb_handle *h, int64_t n_iters);
+
+/* One iteration with every draw supplied by the caller (parity hook):
+ * minibatch edges as slots into nodes[] with y, the step's scale, node ids,
+ * neighbour ids + y per node (n_nodes x (num_node_sample+1)), phi noise
+ * (n_nodes x K), theta noise (K x 2), and the step index used for eps_t.
+ * Does not advance the internal step counter. */
+int ammsb_step_fed(ammsb_handle *h, uint32_t step, int32_t n_edges,
+                   const int32_t *edge_slot_a, const int32_t *edge_slot_b,
+                   const uint8_t *edge_y, float scale, int32_t n_nodes,
+                   const int32_t *nodes, const int32_t *nbrs,
+                   const uint8_t *nbr_y, const float *phi_noise,
+                   const float *theta_noise);
+
+/* Learner::cal_perplexity_held_out (learner.cc:128, 138-183): running
+ * average per held-out edge, -mean log; advances average_count. */
+int ammsb_perplexity(ammsb_handle *h, double *out);
+
+/* MCMCSamplerStochastic::run (cc:93-183): perplexity every interval steps
+ * (printed in the reference's line format on stdout), convergence test
+ * (learner.cc:130-136), until max_iteration.  Returns the last perplexity. */
+int ammsb_run(ammsb_handle *h, double *last_perplexity);
+
+/* State readers (host destination arrays). */
+int ammsb_get_pi(ammsb_handle *h, float *dst);       /* N x K */
+int ammsb_get_phi(ammsb_handle *h, float *dst);      /* N x K */
+int ammsb_get_theta(ammsb_handle *h, double *dst);   /* K x 2 */
+int ammsb_get_beta(ammsb_handle *h, float *dst);     /* K */
+int ammsb_get_ppx(ammsb_handle *h, float *dst);      /* held-out count */
+int ammsb_get_step(ammsb_handle *h, uint64_t *step_count,
+                   uint64_t *average_count);
+int ammsb_set_step(ammsb_handle *h, uint64_t step_count);
+
+/* Draws of the last ammsb_step() iteration, for sampling parity.
+ * sizes: n_edges <= max_edges, n_nodes <= max_nodes; nbrs/nbr_y hold
+ * n_nodes x (num_node_sample + 1). */
+int ammsb_get_last_minibatch(ammsb_handle *h, int32_t *flag, int32_t *n_edges,
+                             int32_t *n_nodes, float *scale,
+                             int32_t *edge_slot_a, int32_t *edge_slot_b,
+                             uint8_t *edge_y, int32_t *nodes, int32_t *nbrs,
+                             uint8_t *nbr_y);
+/* Buffer capacities of the handle. */
+int ammsb_get_sizes(ammsb_handle *h, int64_t *N, int64_t *K,
+                    int64_t *max_edges, int64_t *max_nodes,
+                    int64_t *num_node_sample, int64_t *held_out_count);
+/* Options after the derived defaults were applied. */
+int ammsb_get_options(ammsb_handle *h, ammsb_options *out);
+
+/* Device-side timing of one iteration's phases (milliseconds, CUDA events
+ * on the handle's stream): sample_mini_batch, sample_neighbor_nodes,
+ * update_phi, update_pi + beta gradients, theta.  Mirrors the reference's
+ * per-phase Timers (cc:95-102). */
+int ammsb_profile_step(ammsb_handle *h, double *ms5);
+
+/* Raw stream of the handle (cudaStream_t as void*), for callers that
+ * order their own work against it. */
+void *ammsb_stream(ammsb_handle *h);
+
+/* ------------------------------------------------------------------------ */
+/* Host-side data preparation (no GPU use).                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Synthetic planted-community graph: n nodes, k_true communities with sizes
+ * drawn Zipf(zipf_s) clipped to [size_min, size_max] and rescaled to cover
+ * the memberships; each node joins 1/2/3 communities with probabilities
+ * p1/p2/(1-p1-p2); each community of size s gets round(intra_degree * s / 2)
+ * random member pairs; background_frac * that many uniform pairs are added;
+ * self-loops dropped, duplicates merged.  Philox-seeded. */
+typedef struct ammsb_gen_params {
+  int64_t n;
+  int64_t k_true;
+  double zipf_s;
+  int64_t size_min, size_max;
+  double p1, p2;
+  double intra_degree;
+  double background_frac;
+  uint32_t seed;
+} ammsb_gen_params;
+
+typedef struct ammsb_graph_buf ammsb_graph_buf;
+
+/* Builds a graph; *out owns its arrays until ammsb_graph_free. */
+int ammsb_generate_graph(const ammsb_gen_params *p, ammsb_graph_buf **out);
+/* CSR from an edge list (any order, duplicates and self-loops dropped). */
+int ammsb_graph_from_edges(int64_t n, int64_t n_edges, const int32_t *a,
+                           const int32_t *b, ammsb_graph_buf **out);
+/* Reads a relativity/SNAP text file (relativity.cc:20-200): four header
+ * lines, then "a b" per line.  contiguous != 0 keeps ids as given
+ * (N = max id + 1); otherwise ids are renumbered in ascending order. */
+int ammsb_read_relativity(const char *path, int contiguous,
+                          ammsb_graph_buf **out);
+/* Writes the graph in that format (each undirected edge once, a < b). */
+int ammsb_write_relativity(const ammsb_graph_buf *g, const char *path);
+void ammsb_graph_view(const ammsb_graph_buf *g, ammsb_graph *view);
+void ammsb_graph_free(ammsb_graph_buf *g);
+
+/* Held-out and test sets (network.cc:503-614): held_out_size =
+ * ratio * E; p = held_out_size / 2 random links plus p random non-links for
+ * each set, test disjoint from held-out.  Philox-seeded. */
+typedef struct ammsb_split_buf ammsb_split_buf;
+int ammsb_make_held_out(const ammsb_graph_buf *g, double held_out_ratio,
+                        uint32_t seed, ammsb_split_buf **out);
+void ammsb_split_view(const ammsb_split_buf *s, ammsb_edge_set *held_out,
+                      ammsb_edge_set *test);
+void ammsb_split_free(ammsb_split_buf *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

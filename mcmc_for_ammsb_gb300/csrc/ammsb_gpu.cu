@@ -1,0 +1,918 @@
+// ammsb_gpu.cu -- host driver of the GB300 a-MMSB sampler and its C ABI
+// (include/ammsb_gpu.h).  The handle plays the role of the reference's
+// MCMCSamplerStochastic object (mcmc_sampler_stochastic.h:32-140): it owns
+// phi, pi, theta, beta and the held-out running averages, all resident in
+// GPU memory, and runs the iteration as a captured CUDA graph of the
+// kernels in ammsb_kernels.cuh.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ammsb_gpu.h"
+#include "ammsb_kernels.cuh"
+
+using namespace ammsb;
+
+namespace {
+thread_local std::string g_create_error;
+
+int next_pow2(int64_t v) {
+  int64_t p = 1;
+  while (p < v) p <<= 1;
+  return (int)p;
+}
+
+// Host gamma draw of the same stream layout as gamma_draw() (theta init).
+double host_gamma(const Stream& s, uint32_t tag, uint32_t entity, uint64_t idx,
+                  double shape, double scale) {
+  double a = shape, boost = 1.0;
+  if (a < 1.0) {
+    U32x4 o = s.block(tag, entity, 0xffffffffu, idx);
+    double u = ((double)o.w + 0.5) * 2.3283064365386963e-10;
+    boost = std::pow(u, 1.0 / a);
+    a += 1.0;
+  }
+  const double d = a - 1.0 / 3.0, c = 1.0 / std::sqrt(9.0 * d);
+  for (uint32_t attempt = 0; attempt < 64; ++attempt) {
+    U32x4 o = s.block(tag, entity, attempt, idx);
+    double u1 = ((double)o.x + 0.5) * 2.3283064365386963e-10;
+    double u2 = (double)o.y * 2.3283064365386963e-10;
+    double x = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
+    double v = 1.0 + c * x;
+    if (v <= 0.0) continue;
+    v = v * v * v;
+    double u = ((double)o.z + 0.5) * 2.3283064365386963e-10;
+    if (u < 1.0 - 0.0331 * x * x * x * x) return d * v * boost * scale;
+    if (std::log(u) < 0.5 * x * x + d * (1.0 - v + std::log(v))) return d * v * boost * scale;
+  }
+  return d * boost * scale;
+}
+
+}  // namespace
+
+struct KernelCfg {
+  int lpn, vpl, split, npb;  // update_phi
+  int ppx_lpn, ppx_vpl;      // perplexity
+  int kq;                    // commit_beta
+};
+
+struct ammsb_handle {
+  ammsb_options opt{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Model m{};
+  DevGraph g{};
+  Buffers b{};
+  KernelCfg cfg{};
+  int64_t E = 0, H = 0, T = 0;
+  int pi_bytes = 4;
+  // device allocations
+  std::vector<void*> allocs;
+  int32_t* d_ha = nullptr;
+  int32_t* d_hb = nullptr;
+  uint8_t* d_hy = nullptr;
+  float* d_ppx = nullptr;
+  double* d_ppx_part = nullptr;
+  double* d_ppx_out = nullptr;
+  int ppx_blocks = 1;
+  float* d_fed_phi_noise = nullptr;
+  float* d_fed_theta_noise = nullptr;
+  int32_t* d_err_init = nullptr;
+  int ncommit = 1;
+  int nbr_blocks = 1, phi_blocks = 1;
+  size_t phi_smem = 0, nbr_smem = 0;
+  // host mirrors
+  uint64_t step_count = 1;     // learner.cc:37
+  uint64_t average_count = 1;  // learner.cc:30
+  std::vector<double> ppx_history;
+  bool state_ready = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::string err;
+};
+
+#define CK(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return AMMSB_E_CUDA;                                                    \
+    }                                                                         \
+  } while (0)
+
+namespace {
+
+template <typename T>
+int dev_alloc(ammsb_handle* h, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+  CK(cudaMalloc(&q, bytes));
+  CK(cudaMemsetAsync(q, 0, bytes, h->stream));
+  h->allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return AMMSB_OK;
+}
+
+// ---- kernel dispatch -------------------------------------------------------
+template <typename PiT, int LPN, int VPL, int SPLIT>
+cudaError_t launch_phi_t(ammsb_handle* h, const Buffers& b) {
+  constexpr int NPB = 128 / (LPN * SPLIT) > 0 ? 128 / (LPN * SPLIT) : 1;
+  int blocks = (h->m.max_nodes + NPB - 1) / NPB;
+  blocks = std::max(1, std::min(blocks, 152 * 32));
+  size_t smem = ((size_t)NPB * SPLIT * h->m.Kp + NPB * SPLIT + NPB * std::max(1, SPLIT * LPN / 32)) * sizeof(float);
+  k_update_phi<PiT, LPN, VPL, SPLIT, NPB><<<blocks, NPB * SPLIT * LPN, smem, h->stream>>>(h->m, b);
+  return cudaGetLastError();
+}
+
+template <typename PiT>
+cudaError_t launch_phi(ammsb_handle* h, const Buffers& b) {
+  const KernelCfg& c = h->cfg;
+#define PHI_CASE(L, V, S) \
+  if (c.lpn == L && c.vpl == V && c.split == S) return launch_phi_t<PiT, L, V, S>(h, b);
+  PHI_CASE(1, 1, 1) PHI_CASE(2, 1, 1) PHI_CASE(4, 1, 1) PHI_CASE(8, 1, 1) PHI_CASE(16, 1, 1)
+  PHI_CASE(32, 1, 1) PHI_CASE(32, 1, 2) PHI_CASE(32, 1, 4)
+  PHI_CASE(32, 2, 1) PHI_CASE(32, 2, 2) PHI_CASE(32, 2, 4)
+  PHI_CASE(32, 4, 1) PHI_CASE(32, 4, 2) PHI_CASE(32, 4, 4)
+  PHI_CASE(32, 8, 1) PHI_CASE(32, 8, 2) PHI_CASE(32, 8, 4)
+#undef PHI_CASE
+  return cudaErrorInvalidConfiguration;
+}
+
+template <typename PiT>
+cudaError_t launch_commit(ammsb_handle* h, const Buffers& b) {
+  const int grid = h->ncommit + h->m.nbb;
+  switch (h->cfg.kq) {
+    case 1: k_commit_beta<PiT, 1><<<grid, 128, 0, h->stream>>>(h->m, b, h->ncommit); break;
+    case 2: k_commit_beta<PiT, 2><<<grid, 128, 0, h->stream>>>(h->m, b, h->ncommit); break;
+    case 4: k_commit_beta<PiT, 4><<<grid, 128, 0, h->stream>>>(h->m, b, h->ncommit); break;
+    case 8: k_commit_beta<PiT, 8><<<grid, 128, 0, h->stream>>>(h->m, b, h->ncommit); break;
+    default: return cudaErrorInvalidConfiguration;
+  }
+  return cudaGetLastError();
+}
+
+template <typename PiT>
+cudaError_t launch_ppx(ammsb_handle* h, float count) {
+  const PiT* pi = reinterpret_cast<const PiT*>(h->b.pi);
+  const int nb = h->ppx_blocks;
+#define PPX_CASE(L, V)                                                                         \
+  if (h->cfg.ppx_lpn == L && h->cfg.ppx_vpl == V) {                                            \
+    k_perplexity<PiT, L, V><<<nb, 256, 0, h->stream>>>(h->m, pi, h->b.beta, h->d_ha, h->d_hb, \
+                                                       h->d_hy, h->H, h->d_ppx, count,        \
+                                                       h->d_ppx_part);                        \
+    return cudaGetLastError();                                                                 \
+  }
+  PPX_CASE(1, 1) PPX_CASE(2, 1) PPX_CASE(4, 1) PPX_CASE(8, 1) PPX_CASE(16, 1) PPX_CASE(32, 1)
+  PPX_CASE(32, 2) PPX_CASE(32, 4) PPX_CASE(32, 8)
+#undef PPX_CASE
+  return cudaErrorInvalidConfiguration;
+}
+
+cudaError_t launch_normalize(ammsb_handle* h) {
+  const int blocks = (int)std::min<int64_t>((h->m.N + 7) / 8, 152 * 64);
+  if (h->opt.pi_dtype == AMMSB_PI_BF16)
+    k_normalize_rows<__nv_bfloat16><<<blocks, 256, 0, h->stream>>>(
+        h->m, h->b.phi, reinterpret_cast<__nv_bfloat16*>(h->b.pi));
+  else
+    k_normalize_rows<float><<<blocks, 256, 0, h->stream>>>(h->m, h->b.phi,
+                                                           reinterpret_cast<float*>(h->b.pi));
+  return cudaGetLastError();
+}
+
+// The iteration's kernels in order; `b` carries the fed-noise pointers when
+// called from ammsb_step_fed (which skips the two sampling kernels).
+cudaError_t launch_update_phase(ammsb_handle* h, const Buffers& b) {
+  cudaError_t e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_phi<__nv_bfloat16>(h, b)
+                                                      : launch_phi<float>(h, b);
+  if (e != cudaSuccess) return e;
+  e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_commit<__nv_bfloat16>(h, b)
+                                          : launch_commit<float>(h, b);
+  if (e != cudaSuccess) return e;
+  k_theta<<<(h->m.K + 255) / 256, 256, 0, h->stream>>>(h->m, b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sampling_phase(ammsb_handle* h) {
+  k_sample_minibatch<<<1, 1024, 0, h->stream>>>(h->m, h->g, h->b);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, h->stream>>>(h->m, h->g, h->b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_iteration(ammsb_handle* h) {
+  cudaError_t e = launch_sampling_phase(h);
+  if (e != cudaSuccess) return e;
+  return launch_update_phase(h, h->b);
+}
+
+int check_device_err(ammsb_handle* h) {
+  DevState st;
+  CK(cudaMemcpyAsync(&st, h->b.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (st.err) {
+    h->err = "device sampling error bits " + std::to_string(st.err);
+    if (st.err & kErrCapacity) return AMMSB_E_CAPACITY;
+    return AMMSB_E_SAMPLING;
+  }
+  return AMMSB_OK;
+}
+
+int reset_counters(ammsb_handle* h) {
+  h->step_count = 1;
+  h->average_count = 1;
+  h->ppx_history.clear();
+  DevState st{};
+  st.next_step = 1;
+  st.step = 1;
+  CK(cudaMemcpyAsync(h->b.st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemsetAsync(h->d_ppx, 0, sizeof(float) * std::max<int64_t>(h->H, 1), h->stream));
+  return AMMSB_OK;
+}
+
+void choose_config(ammsb_handle* h) {
+  const int ev = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 8 : 4;
+  const int nvec = h->m.Kp / ev;
+  KernelCfg c{};
+  if (nvec <= 32) {
+    c.lpn = std::min(32, next_pow2(nvec));
+    c.vpl = 1;
+  } else {
+    c.lpn = 32;
+    c.vpl = next_pow2((nvec + 31) / 32);
+  }
+  c.split = (c.lpn == 32) ? (c.vpl >= 2 ? 4 : 2) : 1;
+  c.npb = std::max(1, 128 / (c.lpn * c.split));
+  c.ppx_lpn = c.lpn;
+  c.ppx_vpl = c.vpl;
+  c.kq = std::max(1, next_pow2((h->m.Kp + 127) / 128));
+  h->cfg = c;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ammsb_options_default(ammsb_options* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->alpha = 0.0;
+  o->eta0 = 1.0;
+  o->eta1 = 1.0;
+  o->epsilon = 0.0000001;
+  o->a = 0.0;
+  o->b = 1024;
+  o->c = 0.5;
+  o->K = 300;
+  o->mini_batch_size = 0;
+  o->num_node_sample = 0;
+  o->strategy = AMMSB_STRATIFIED_RANDOM_NODE;
+  o->sampler_max_source = 1;
+  o->max_iteration = 10000000;
+  o->interval = 0;
+  o->stats_print_interval = 0;
+  o->num_updates = 1000;
+  o->held_out_ratio = 0.0;
+  o->random_seed = 42;
+  o->convergence_threshold = 0.000000000001;
+  o->pi_dtype = AMMSB_PI_F32;
+  o->chain = 0;
+  o->device = 0;
+  o->use_graph = 1;
+  o->verbose = 0;
+}
+
+const char* ammsb_create_error(void) { return g_create_error.c_str(); }
+
+const char* ammsb_last_error(const ammsb_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+void ammsb_destroy(ammsb_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
+                 const ammsb_edge_set* held_out, const ammsb_edge_set* test,
+                 ammsb_handle** out) {
+  g_create_error.clear();
+  auto fail = [](const std::string& msg, int code) {
+    g_create_error = msg;
+    return code;
+  };
+  if (!opt_in || !graph || !out) return fail("null argument", AMMSB_E_ARG);
+  *out = nullptr;
+  ammsb_options o = *opt_in;
+  const int64_t N = graph->n;
+  if (N < 2 || N > INT32_MAX || !graph->row_ptr || (!graph->col && graph->row_ptr[N] > 0))
+    return fail("graph: need 2 <= n <= 2^31-1 and CSR arrays", AMMSB_E_ARG);
+  if (o.K < 1 || o.K > 1024) return fail("K must be in [1, 1024]", AMMSB_E_ARG);
+  if (o.strategy < 0 || o.strategy > 3) return fail("Invalid sampling strategy", AMMSB_E_ARG);
+  if (o.strategy == AMMSB_RANDOM_EDGE)
+    return fail("strategy random-edge is not implemented on the GPU path", AMMSB_E_UNSUPPORTED);
+  if (o.sampler_max_source != 1)
+    return fail("sampler.max-source > 1 is not implemented on the GPU path", AMMSB_E_UNSUPPORTED);
+  if (o.pi_dtype != AMMSB_PI_F32 && o.pi_dtype != AMMSB_PI_BF16)
+    return fail("pi_dtype must be AMMSB_PI_F32 or AMMSB_PI_BF16", AMMSB_E_ARG);
+  // derived defaults: options.h:257-262, learner.cc:88-92, cc:15-24, 35-44
+  if (o.a == 0.0) o.a = std::pow(o.b, -o.c);
+  if (o.alpha == 0.0) o.alpha = 1.0 / (double)o.K;
+  if (o.held_out_ratio == 0.0) o.held_out_ratio = 0.1;
+  if (o.interval == 0) o.interval = 50;
+  if (o.stats_print_interval == 0) o.stats_print_interval = 64 * 1024;
+  if (o.num_node_sample == 0) o.num_node_sample = N / 50;
+  if (o.mini_batch_size == 0) o.mini_batch_size = N / 10;
+  if (o.num_node_sample < 1 || o.num_node_sample + 1 > N - 1)
+    return fail("num_node_sample must be in [1, N-2]", AMMSB_E_ARG);
+  if (o.mini_batch_size < 1 || o.mini_batch_size > N - 1 || o.mini_batch_size > (1 << 24))
+    return fail("mini_batch_size must be in [1, min(N-1, 2^24)]", AMMSB_E_ARG);
+  if (o.b <= 0 || o.epsilon <= 0 || o.epsilon >= 1) return fail("invalid b or epsilon", AMMSB_E_ARG);
+
+  // validate the CSR: monotone row_ptr, ids in range, sorted rows, no self loops
+  const int64_t nnz = graph->row_ptr[N];
+  if (graph->row_ptr[0] != 0 || nnz < 0 || (nnz & 1)) return fail("graph: bad row_ptr", AMMSB_E_ARG);
+  int64_t maxdeg = 0;
+  for (int64_t v = 0; v < N; ++v) {
+    const int64_t r0 = graph->row_ptr[v], r1 = graph->row_ptr[v + 1];
+    if (r1 < r0 || r1 > nnz) return fail("graph: row_ptr not monotone", AMMSB_E_ARG);
+    maxdeg = std::max(maxdeg, r1 - r0);
+    for (int64_t q = r0; q < r1; ++q) {
+      const int32_t c = graph->col[q];
+      if (c < 0 || c >= N || c == v || (q > r0 && graph->col[q - 1] >= c))
+        return fail("graph: rows must be sorted, in range, without self-loops", AMMSB_E_ARG);
+    }
+  }
+  auto check_set = [&](const ammsb_edge_set* s) {
+    if (!s || s->count == 0) return true;
+    if (s->count < 0 || !s->a || !s->b || !s->y) return false;
+    for (int64_t i = 0; i < s->count; ++i)
+      if (s->a[i] < 0 || s->b[i] < 0 || s->a[i] >= N || s->b[i] >= N || s->a[i] == s->b[i])
+        return false;
+    return true;
+  };
+  if (!check_set(held_out) || !check_set(test)) return fail("held-out/test sets: bad pairs", AMMSB_E_ARG);
+
+  auto* h = new ammsb_handle();
+  h->opt = o;
+  h->device = o.device;
+  h->E = nnz / 2;
+  h->H = held_out ? held_out->count : 0;
+  h->T = test ? test->count : 0;
+  auto bail = [&](int code) {
+    g_create_error = h->err;
+    ammsb_destroy(h);
+    return code;
+  };
+  if (cudaSetDevice(o.device) != cudaSuccess) {
+    h->err = "cudaSetDevice failed (no CUDA device?)";
+    return bail(AMMSB_E_CUDA);
+  }
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    h->err = "cudaStreamCreate failed";
+    return bail(AMMSB_E_CUDA);
+  }
+  const int K = (int)o.K;
+  h->pi_bytes = (o.pi_dtype == AMMSB_PI_BF16) ? 2 : 4;
+  const int Kp = (o.pi_dtype == AMMSB_PI_BF16) ? ((K + 7) / 8) * 8 : ((K + 3) / 4) * 4;
+  Model& m = h->m;
+  m.K = K;
+  m.Kp = Kp;
+  m.N = N;
+  m.alpha = (float)o.alpha;
+  m.epsilon = (float)o.epsilon;
+  m.Nn = (1.0f * (float)N) / (float)o.num_node_sample;
+  m.eta0 = (float)o.eta0;
+  m.eta1 = (float)o.eta1;
+  m.a = o.a;
+  m.b = o.b;
+  m.c = o.c;
+  m.seed = (uint32_t)o.random_seed;
+  m.chain = (uint32_t)o.chain;
+  m.n_out = (int32_t)o.num_node_sample + 1;
+  const int64_t max_edges = std::max<int64_t>(o.mini_batch_size, std::max<int64_t>(maxdeg, 1));
+  m.max_edges = (int32_t)max_edges;
+  m.max_nodes = (int32_t)(max_edges + 1);
+  m.mini_batch_size = (int32_t)o.mini_batch_size;
+  m.strategy = o.strategy;
+  {  // network.cc:341-342 with Float = float
+    float scale = (float)N * (float)N / (float)o.mini_batch_size;
+    scale = (float)((double)scale * ((double)h->E / ((double)N * ((double)N - 1.0) / 2.0 - (double)h->E)));
+    m.nonlink_scale = scale;
+    m.link_scale = (float)N;  // network.cc:386-387, max-source 1
+  }
+  m.nbb = (int)std::min<int64_t>(256, std::max<int64_t>(1, (max_edges + 3) / 4));
+  choose_config(h);
+  if (h->cfg.vpl > 8) {
+    h->err = "K too large for the row kernels";
+    return bail(AMMSB_E_ARG);
+  }
+
+  Buffers& b = h->b;
+  DevGraph& g = h->g;
+  int rc = AMMSB_OK;
+  int64_t* d_row = nullptr;
+  int32_t* d_col = nullptr;
+#define TRY(x)                   \
+  do {                           \
+    rc = (x);                    \
+    if (rc != AMMSB_OK) return bail(rc); \
+  } while (0)
+  TRY(dev_alloc(h, &d_row, N + 1));
+  TRY(dev_alloc(h, &d_col, std::max<int64_t>(nnz, 1)));
+  if (cudaMemcpyAsync(d_row, graph->row_ptr, sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      (nnz > 0 && cudaMemcpyAsync(d_col, graph->col, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)) {
+    h->err = "graph upload failed";
+    return bail(AMMSB_E_CUDA);
+  }
+  g.n = N;
+  g.row_ptr = d_row;
+  g.col = d_col;
+  {  // held-out + test exclusion hash
+    const int64_t nex = h->H + h->T;
+    const int cap = next_pow2(std::max<int64_t>(16, 2 * nex));
+    std::vector<unsigned long long> keys(cap, kEmptyKey);
+    auto insert = [&](const ammsb_edge_set* s) {
+      if (!s) return;
+      for (int64_t i = 0; i < s->count; ++i) {
+        unsigned long long k = pair_key(s->a[i], s->b[i]);
+        uint32_t slot = hash64(k) & (uint32_t)(cap - 1);
+        while (keys[slot] != kEmptyKey && keys[slot] != k) slot = (slot + 1) & (uint32_t)(cap - 1);
+        keys[slot] = k;
+      }
+    };
+    insert(held_out);
+    insert(test);
+    unsigned long long* d_ex = nullptr;
+    TRY(dev_alloc(h, &d_ex, cap));
+    if (cudaMemcpyAsync(d_ex, keys.data(), sizeof(unsigned long long) * cap, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) {
+      h->err = "exclusion upload failed";
+      return bail(AMMSB_E_CUDA);
+    }
+    g.excl = d_ex;
+    g.excl_mask = (uint32_t)(cap - 1);
+  }
+  // held-out set for perplexity
+  TRY(dev_alloc(h, &h->d_ha, std::max<int64_t>(h->H, 1)));
+  TRY(dev_alloc(h, &h->d_hb, std::max<int64_t>(h->H, 1)));
+  TRY(dev_alloc(h, &h->d_hy, std::max<int64_t>(h->H, 1)));
+  TRY(dev_alloc(h, &h->d_ppx, std::max<int64_t>(h->H, 1)));
+  if (h->H > 0) {
+    if (cudaMemcpyAsync(h->d_ha, held_out->a, sizeof(int32_t) * h->H, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+        cudaMemcpyAsync(h->d_hb, held_out->b, sizeof(int32_t) * h->H, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+        cudaMemcpyAsync(h->d_hy, held_out->y, h->H, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) {
+      h->err = "held-out upload failed";
+      return bail(AMMSB_E_CUDA);
+    }
+  }
+  {
+    const int gpb = 256 / h->cfg.ppx_lpn;
+    h->ppx_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((h->H + gpb - 1) / gpb, 152 * 8));
+  }
+  TRY(dev_alloc(h, &h->d_ppx_part, 2 * (size_t)h->ppx_blocks));
+  TRY(dev_alloc(h, &h->d_ppx_out, 1));
+  // model state
+  void* d_pi = nullptr;
+  {
+    void* q = nullptr;
+    const size_t bytes = (size_t)N * Kp * h->pi_bytes;
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+      h->err = "cudaMalloc pi failed";
+      return bail(AMMSB_E_CUDA);
+    }
+    h->allocs.push_back(q);
+    cudaMemsetAsync(q, 0, bytes, h->stream);
+    d_pi = q;
+  }
+  b.pi = d_pi;
+  TRY(dev_alloc(h, &b.phi, (size_t)N * Kp));
+  TRY(dev_alloc(h, &b.stage, (size_t)m.max_nodes * Kp));
+  TRY(dev_alloc(h, &b.beta, (size_t)Kp));
+  TRY(dev_alloc(h, &b.theta, 2 * (size_t)K));
+  TRY(dev_alloc(h, &b.nodes, (size_t)m.max_nodes));
+  TRY(dev_alloc(h, &b.ea, (size_t)m.max_edges));
+  TRY(dev_alloc(h, &b.eb, (size_t)m.max_edges));
+  TRY(dev_alloc(h, &b.ey, (size_t)m.max_edges));
+  TRY(dev_alloc(h, &b.nbr, (size_t)m.max_nodes * m.n_out));
+  TRY(dev_alloc(h, &b.cand, (size_t)o.mini_batch_size));
+  const int hcap = next_pow2(std::max<int64_t>(64, 2 * o.mini_batch_size));
+  TRY(dev_alloc(h, &b.htab_key, (size_t)hcap));
+  TRY(dev_alloc(h, &b.htab_idx, (size_t)hcap));
+  b.hmask = (uint32_t)(hcap - 1);
+  TRY(dev_alloc(h, &b.beta_part, (size_t)m.nbb * 2 * Kp));
+  TRY(dev_alloc(h, &b.st, 1));
+  TRY(dev_alloc(h, &h->d_err_init, 1));
+  TRY(dev_alloc(h, &h->d_fed_phi_noise, (size_t)m.max_nodes * K));
+  TRY(dev_alloc(h, &h->d_fed_theta_noise, 2 * (size_t)K));
+  b.fed_phi_noise = nullptr;
+  b.fed_theta_noise = nullptr;
+#undef TRY
+  h->ncommit = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 3) / 4, 152 * 8));
+  h->nbr_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 7) / 8, 152 * 8));
+  h->nbr_smem = (size_t)8 * m.n_out * sizeof(int32_t);
+  if (h->nbr_smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(k_sample_neighbors<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)h->nbr_smem) != cudaSuccess) {
+      h->err = "num_node_sample too large for the neighbour kernel";
+      return bail(AMMSB_E_ARG);
+    }
+  }
+  if (reset_counters(h) != AMMSB_OK) return bail(AMMSB_E_CUDA);
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    h->err = std::string("create: ") + cudaGetErrorString(cudaGetLastError());
+    return bail(AMMSB_E_CUDA);
+  }
+  if (o.verbose) {
+    std::fprintf(stderr, "N %lld E %lld K %d\nminibatch size %lld epsilon %g alpha %g iterations %lld\n",
+                 (long long)N, (long long)h->E, K, (long long)o.mini_batch_size, o.epsilon, o.alpha,
+                 (long long)o.max_iteration);
+    std::fprintf(stderr, "num_node_sample %lld\na %g b %g c %g eta (%g,%g)\n",
+                 (long long)o.num_node_sample, o.a, o.b, o.c, o.eta0, o.eta1);
+    std::fprintf(stderr, "update_phi lanes/node %d vec/lane %d split %d; pi %s\n", h->cfg.lpn,
+                 h->cfg.vpl, h->cfg.split, o.pi_dtype == AMMSB_PI_BF16 ? "bf16" : "f32");
+  }
+  *out = h;
+  return AMMSB_OK;
+}
+
+int ammsb_init_state(ammsb_handle* h) {
+  if (!h) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  const int K = h->m.K;
+  const Stream rs{h->m.seed, h->m.chain};
+  std::vector<double> theta(2 * (size_t)K);
+  std::vector<float> beta(h->m.Kp, 0.f);
+  for (int k = 0; k < K; ++k) {  // theta = gamma(eta0, eta1, K, 2), cc:54
+    theta[2 * k] = host_gamma(rs, kTagThetaInit, 0, 2ull * k, h->opt.eta0, h->opt.eta1);
+    theta[2 * k + 1] = host_gamma(rs, kTagThetaInit, 0, 2ull * k + 1, h->opt.eta0, h->opt.eta1);
+    beta[k] = (float)(theta[2 * k + 1] / (theta[2 * k] + theta[2 * k + 1]));
+  }
+  CK(cudaMemcpyAsync(h->b.theta, theta.data(), sizeof(double) * 2 * K, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->b.beta, beta.data(), sizeof(float) * h->m.Kp, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemsetAsync(h->d_err_init, 0, sizeof(int32_t), h->stream));
+  const int64_t total = h->m.N * (int64_t)h->m.Kp;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 64));
+  k_init_phi<<<blocks, 256, 0, h->stream>>>(h->m, h->b.phi, 1.0, 1.0, h->d_err_init);  // cc:66
+  CK(cudaGetLastError());
+  CK(launch_normalize(h));
+  int rc = reset_counters(h);
+  if (rc) return rc;
+  int32_t err = 0;
+  CK(cudaMemcpyAsync(&err, h->d_err_init, sizeof(err), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (err) {
+    h->err = "gamma initialisation hit its rejection cap";
+    return AMMSB_E_SAMPLING;
+  }
+  h->state_ready = true;
+  return AMMSB_OK;
+}
+
+int ammsb_set_state(ammsb_handle* h, const float* phi, const double* theta) {
+  if (!h || !phi || !theta) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  const int K = h->m.K, Kp = h->m.Kp;
+  for (int64_t x = 0; x < h->m.N * (int64_t)K; ++x)
+    if (!(phi[x] > 0.f) || !std::isfinite(phi[x])) {
+      h->err = "phi must be positive and finite";
+      return AMMSB_E_ARG;
+    }
+  std::vector<float> beta(Kp, 0.f);
+  for (int k = 0; k < K; ++k) {
+    if (!(theta[2 * k] > 0) || !(theta[2 * k + 1] > 0)) {
+      h->err = "theta must be positive";
+      return AMMSB_E_ARG;
+    }
+    beta[k] = (float)(theta[2 * k + 1] / (theta[2 * k] + theta[2 * k + 1]));
+  }
+  CK(cudaMemcpy2DAsync(h->b.phi, sizeof(float) * Kp, phi, sizeof(float) * K, sizeof(float) * K, h->m.N,
+                       cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->b.theta, theta, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->b.beta, beta.data(), sizeof(float) * Kp, cudaMemcpyHostToDevice, h->stream));
+  CK(launch_normalize(h));
+  int rc = reset_counters(h);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  h->state_ready = true;
+  return AMMSB_OK;
+}
+
+int ammsb_set_step(ammsb_handle* h, uint64_t step_count) {
+  if (!h || step_count < 1 || step_count > 0xffffffffull) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  h->step_count = step_count;
+  uint32_t s = (uint32_t)step_count;
+  CK(cudaMemcpyAsync(&h->b.st->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return AMMSB_OK;
+}
+
+int ammsb_step(ammsb_handle* h, int64_t n_iters) {
+  if (!h || n_iters < 0) return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    h->err = "call ammsb_init_state or ammsb_set_state first";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  if (h->opt.use_graph && !h->graph_exec && n_iters > 0) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = launch_iteration(h);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+      return AMMSB_E_CUDA;
+    }
+    CK(cudaGraphInstantiate(&h->graph_exec, graph, 0));
+    cudaGraphDestroy(graph);
+  }
+  for (int64_t it = 0; it < n_iters; ++it) {
+    if (h->graph_exec)
+      CK(cudaGraphLaunch(h->graph_exec, h->stream));
+    else
+      CK(launch_iteration(h));
+  }
+  h->step_count += (uint64_t)n_iters;
+  return AMMSB_OK;
+}
+
+int ammsb_step_fed(ammsb_handle* h, uint32_t step, int32_t n_edges, const int32_t* edge_slot_a,
+                   const int32_t* edge_slot_b, const uint8_t* edge_y, float scale, int32_t n_nodes,
+                   const int32_t* nodes, const int32_t* nbrs, const uint8_t* nbr_y,
+                   const float* phi_noise, const float* theta_noise) {
+  if (!h || n_edges < 0 || n_nodes < 1 || !nodes || !nbrs || !nbr_y || !phi_noise || !theta_noise ||
+      (n_edges > 0 && (!edge_slot_a || !edge_slot_b || !edge_y)))
+    return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    h->err = "call ammsb_init_state or ammsb_set_state first";
+    return AMMSB_E_STATE;
+  }
+  if (n_edges > h->m.max_edges || n_nodes > h->m.max_nodes) {
+    h->err = "fed minibatch exceeds the handle's buffers";
+    return AMMSB_E_CAPACITY;
+  }
+  const int n_out = h->m.n_out, K = h->m.K;
+  for (int32_t s = 0; s < n_nodes; ++s)
+    if (nodes[s] < 0 || nodes[s] >= h->m.N) {
+      h->err = "fed node id out of range";
+      return AMMSB_E_ARG;
+    }
+  for (int32_t e = 0; e < n_edges; ++e)
+    if (edge_slot_a[e] < 0 || edge_slot_a[e] >= n_nodes || edge_slot_b[e] < 0 || edge_slot_b[e] >= n_nodes) {
+      h->err = "fed edge slot out of range";
+      return AMMSB_E_ARG;
+    }
+  std::vector<uint32_t> packed((size_t)n_nodes * n_out);
+  for (size_t q = 0; q < packed.size(); ++q) {
+    if (nbrs[q] < 0 || nbrs[q] >= h->m.N) {
+      h->err = "fed neighbour id out of range";
+      return AMMSB_E_ARG;
+    }
+    packed[q] = (uint32_t)nbrs[q] | ((nbr_y[q] ? 1u : 0u) << 31);
+  }
+  CK(cudaSetDevice(h->device));
+  CK(cudaMemcpyAsync(h->b.nodes, nodes, sizeof(int32_t) * n_nodes, cudaMemcpyHostToDevice, h->stream));
+  if (n_edges > 0) {
+    CK(cudaMemcpyAsync(h->b.ea, edge_slot_a, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->b.eb, edge_slot_b, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->b.ey, edge_y, n_edges, cudaMemcpyHostToDevice, h->stream));
+  }
+  CK(cudaMemcpyAsync(h->b.nbr, packed.data(), sizeof(uint32_t) * packed.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_fed_phi_noise, phi_noise, sizeof(float) * (size_t)n_nodes * K, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_fed_theta_noise, theta_noise, sizeof(float) * 2 * K, cudaMemcpyHostToDevice, h->stream));
+  DevState st{};
+  st.step = step;
+  st.next_step = (uint32_t)h->step_count;
+  st.eps = (float)(h->m.a * std::pow(1.0 + (double)step / h->m.b, -h->m.c));
+  st.scale = scale;
+  st.flag = -1;
+  st.n_edges = n_edges;
+  st.n_nodes = n_nodes;
+  CK(cudaMemcpyAsync(h->b.st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  Buffers fb = h->b;
+  fb.fed_phi_noise = h->d_fed_phi_noise;
+  fb.fed_theta_noise = h->d_fed_theta_noise;
+  CK(launch_update_phase(h, fb));
+  return check_device_err(h);
+}
+
+int ammsb_perplexity(ammsb_handle* h, double* out) {
+  if (!h || !out) return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    h->err = "call ammsb_init_state or ammsb_set_state first";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  const float count = (float)h->average_count;
+  if (h->H > 0) {
+    CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_ppx<__nv_bfloat16>(h, count) : launch_ppx<float>(h, count));
+  }
+  k_ppx_final<<<1, 32, 0, h->stream>>>(h->d_ppx_part, h->H > 0 ? h->ppx_blocks : 0, h->H, h->d_ppx_out);
+  CK(cudaGetLastError());
+  double v = 0.0;
+  CK(cudaMemcpyAsync(&v, h->d_ppx_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  int rc = check_device_err(h);  // synchronises
+  if (rc) return rc;
+  h->average_count++;
+  *out = v;
+  return AMMSB_OK;
+}
+
+int ammsb_run(ammsb_handle* h, double* last) {
+  if (!h) return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    int rc = ammsb_init_state(h);
+    if (rc) return rc;
+  }
+  const auto t0 = std::chrono::system_clock::now();
+  double ppx = 0.0;
+  auto converged = [&]() {  // learner.cc:130-136
+    const size_t n = h->ppx_history.size();
+    if (n < 2) return false;
+    return std::fabs(h->ppx_history[n - 1] - h->ppx_history[n - 2]) / h->ppx_history[n - 2] <=
+           h->opt.convergence_threshold;
+  };
+  while (h->step_count < (uint64_t)h->opt.max_iteration && !converged()) {
+    if ((h->step_count - 1) % (uint64_t)h->opt.interval == 0) {
+      int rc = ammsb_perplexity(h, &ppx);
+      if (rc) return rc;
+      const double secs =
+          std::chrono::duration<double>(std::chrono::system_clock::now() - t0).count();
+      std::printf("average_count is: %llu step count: %llu time: %.3f perplexity for hold out set: %.12f\n",
+                  (unsigned long long)(h->average_count - 1), (unsigned long long)h->step_count, secs, ppx);
+      std::fflush(stdout);
+      h->ppx_history.push_back(ppx);
+    }
+    // run up to the next perplexity point
+    const uint64_t interval = (uint64_t)h->opt.interval;
+    uint64_t until = ((h->step_count - 1) / interval + 1) * interval + 1;
+    until = std::min<uint64_t>(until, (uint64_t)h->opt.max_iteration);
+    const int64_t n = (int64_t)(until - h->step_count);
+    int rc = ammsb_step(h, std::max<int64_t>(n, 1));
+    if (rc) return rc;
+  }
+  int rc = check_device_err(h);
+  if (rc) return rc;
+  if (last) *last = ppx;
+  return AMMSB_OK;
+}
+
+int ammsb_get_pi(ammsb_handle* h, float* dst) {
+  if (!h || !dst) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  const int K = h->m.K, Kp = h->m.Kp;
+  const int64_t N = h->m.N;
+  if (h->opt.pi_dtype == AMMSB_PI_F32) {
+    CK(cudaMemcpy2DAsync(dst, sizeof(float) * K, h->b.pi, sizeof(float) * Kp, sizeof(float) * K, N,
+                         cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  } else {
+    std::vector<uint16_t> tmp((size_t)N * K);
+    CK(cudaMemcpy2DAsync(tmp.data(), 2 * K, h->b.pi, 2 * Kp, 2 * K, N, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t x = 0; x < tmp.size(); ++x) {
+      uint32_t u = (uint32_t)tmp[x] << 16;
+      std::memcpy(dst + x, &u, 4);
+    }
+  }
+  return AMMSB_OK;
+}
+
+int ammsb_get_phi(ammsb_handle* h, float* dst) {
+  if (!h || !dst) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  const int K = h->m.K, Kp = h->m.Kp;
+  CK(cudaMemcpy2DAsync(dst, sizeof(float) * K, h->b.phi, sizeof(float) * Kp, sizeof(float) * K, h->m.N,
+                       cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return AMMSB_OK;
+}
+
+int ammsb_get_theta(ammsb_handle* h, double* dst) {
+  if (!h || !dst) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaMemcpyAsync(dst, h->b.theta, sizeof(double) * 2 * h->m.K, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return AMMSB_OK;
+}
+
+int ammsb_get_beta(ammsb_handle* h, float* dst) {
+  if (!h || !dst) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaMemcpyAsync(dst, h->b.beta, sizeof(float) * h->m.K, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return AMMSB_OK;
+}
+
+int ammsb_get_ppx(ammsb_handle* h, float* dst) {
+  if (!h || !dst) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  if (h->H > 0) CK(cudaMemcpyAsync(dst, h->d_ppx, sizeof(float) * h->H, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return AMMSB_OK;
+}
+
+int ammsb_get_step(ammsb_handle* h, uint64_t* step_count, uint64_t* average_count) {
+  if (!h) return AMMSB_E_ARG;
+  if (step_count) *step_count = h->step_count;
+  if (average_count) *average_count = h->average_count;
+  return AMMSB_OK;
+}
+
+int ammsb_get_last_minibatch(ammsb_handle* h, int32_t* flag, int32_t* n_edges, int32_t* n_nodes,
+                             float* scale, int32_t* ea, int32_t* eb, uint8_t* ey, int32_t* nodes,
+                             int32_t* nbrs, uint8_t* nbr_y) {
+  if (!h) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  DevState st;
+  CK(cudaMemcpyAsync(&st, h->b.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (flag) *flag = st.flag;
+  if (n_edges) *n_edges = st.n_edges;
+  if (n_nodes) *n_nodes = st.n_nodes;
+  if (scale) *scale = st.scale;
+  if (st.n_edges > 0) {
+    if (ea) CK(cudaMemcpyAsync(ea, h->b.ea, sizeof(int32_t) * st.n_edges, cudaMemcpyDeviceToHost, h->stream));
+    if (eb) CK(cudaMemcpyAsync(eb, h->b.eb, sizeof(int32_t) * st.n_edges, cudaMemcpyDeviceToHost, h->stream));
+    if (ey) CK(cudaMemcpyAsync(ey, h->b.ey, st.n_edges, cudaMemcpyDeviceToHost, h->stream));
+  }
+  if (st.n_nodes > 0) {
+    if (nodes) CK(cudaMemcpyAsync(nodes, h->b.nodes, sizeof(int32_t) * st.n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    if (nbrs || nbr_y) {
+      std::vector<uint32_t> packed((size_t)st.n_nodes * h->m.n_out);
+      CK(cudaMemcpyAsync(packed.data(), h->b.nbr, sizeof(uint32_t) * packed.size(), cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      for (size_t q = 0; q < packed.size(); ++q) {
+        if (nbrs) nbrs[q] = (int32_t)(packed[q] & 0x7fffffffu);
+        if (nbr_y) nbr_y[q] = (uint8_t)(packed[q] >> 31);
+      }
+    }
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  if (st.err) {
+    h->err = "device sampling error bits " + std::to_string(st.err);
+    return (st.err & kErrCapacity) ? AMMSB_E_CAPACITY : AMMSB_E_SAMPLING;
+  }
+  return AMMSB_OK;
+}
+
+int ammsb_get_sizes(ammsb_handle* h, int64_t* N, int64_t* K, int64_t* max_edges, int64_t* max_nodes,
+                    int64_t* num_node_sample, int64_t* held_out_count) {
+  if (!h) return AMMSB_E_ARG;
+  if (N) *N = h->m.N;
+  if (K) *K = h->m.K;
+  if (max_edges) *max_edges = h->m.max_edges;
+  if (max_nodes) *max_nodes = h->m.max_nodes;
+  if (num_node_sample) *num_node_sample = h->opt.num_node_sample;
+  if (held_out_count) *held_out_count = h->H;
+  return AMMSB_OK;
+}
+
+int ammsb_get_options(ammsb_handle* h, ammsb_options* out) {
+  if (!h || !out) return AMMSB_E_ARG;
+  *out = h->opt;
+  return AMMSB_OK;
+}
+
+int ammsb_profile_step(ammsb_handle* h, double* ms5) {
+  if (!h || !ms5) return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    h->err = "call ammsb_init_state or ammsb_set_state first";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  cudaEvent_t ev[6];
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  CK(cudaEventRecord(ev[0], h->stream));
+  k_sample_minibatch<<<1, 1024, 0, h->stream>>>(h->m, h->g, h->b);
+  CK(cudaEventRecord(ev[1], h->stream));
+  k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, h->stream>>>(h->m, h->g, h->b);
+  CK(cudaEventRecord(ev[2], h->stream));
+  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_phi<__nv_bfloat16>(h, h->b) : launch_phi<float>(h, h->b));
+  CK(cudaEventRecord(ev[3], h->stream));
+  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_commit<__nv_bfloat16>(h, h->b) : launch_commit<float>(h, h->b));
+  CK(cudaEventRecord(ev[4], h->stream));
+  k_theta<<<(h->m.K + 255) / 256, 256, 0, h->stream>>>(h->m, h->b);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ev[5], h->stream));
+  CK(cudaEventSynchronize(ev[5]));
+  for (int i = 0; i < 5; ++i) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+    ms5[i] = ms;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  h->step_count += 1;
+  return check_device_err(h);
+}
+
+void* ammsb_stream(ammsb_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,788 @@
+// ammsb_kernels.cuh -- sm_103a kernels of one SG-MCMC iteration.
+//
+// Phase order of MCMCSamplerStochastic::run (mcmc_sampler_stochastic.cc
+// :131-174), one kernel each, all reading the per-iteration scalars from
+// DevState so the sequence replays as a CUDA graph:
+//   k_sample_minibatch   Network::sample_mini_batch + nodes_in_batch
+//   k_sample_neighbors   sample_neighbor_nodes (h:87-108) + y lookups
+//   k_update_phi         update_phi (cc:269-313), fused with the noise draw
+//                        and the normalisation pi_i = phi_i / sum(phi_i)
+//                        into a staging buffer (Jacobi: pi is not touched)
+//   k_commit_beta        pi[nodes] = staged rows (cc:162-166) and the
+//                        per-edge update_beta gradient (cc:212-240) as a
+//                        segmented block reduction
+//   k_theta              sum of block partials + SGRLD theta step + beta
+//                        (cc:244-266), FP64
+#pragma once
+#include "ammsb_device.cuh"
+
+namespace ammsb {
+
+struct Model {
+  int32_t K;      // communities
+  int32_t Kp;     // row stride in elements (K rounded up to 16 bytes)
+  int64_t N;
+  float alpha, epsilon;
+  float Nn;       // N / num_node_sample, as the reference (cc:300)
+  float eta0, eta1;
+  double a, b, c; // step-size schedule
+  uint32_t seed, chain;
+  int32_t n_out;  // num_node_sample + 1 neighbours per node
+  int32_t max_nodes, max_edges;
+  int32_t mini_batch_size;
+  int32_t strategy;
+  float nonlink_scale, link_scale;
+  int32_t nbb;    // beta partial blocks
+};
+
+struct Buffers {
+  void* pi;            // N x Kp, PiT
+  float* phi;          // N x Kp
+  float* stage;        // max_nodes x Kp: new pi rows of the minibatch nodes
+  float* beta;         // K
+  double* theta;       // K x 2
+  int32_t* nodes;      // max_nodes
+  int32_t* ea;         // max_edges: slot of first endpoint
+  int32_t* eb;         // slot of second endpoint
+  uint8_t* ey;         // y of each minibatch edge
+  uint32_t* nbr;       // max_nodes x n_out: id | y << 31
+  int32_t* cand;       // mini_batch_size: candidate scratch
+  uint32_t* htab_key;  // minibatch dedup hash
+  uint32_t* htab_idx;
+  uint32_t hmask;
+  float* beta_part;    // nbb x 2 x Kp
+  const float* fed_phi_noise;    // max_nodes x K or null
+  const float* fed_theta_noise;  // K x 2 or null
+  DevState* st;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Mask of the aligned group of G lanes (G a power of two <= 32) holding
+// `lane`.
+template <int G>
+__device__ __forceinline__ uint32_t group_mask(int lane) {
+  if constexpr (G >= 32) {
+    return 0xffffffffu;
+  } else {
+    return ((1u << G) - 1u) << ((lane / G) * G);
+  }
+}
+
+// Exclusive prefix count of `flag` over a 1024-thread block, in thread
+// order; returns the position and sets *total.  Uses s_warp[32].
+__device__ __forceinline__ int block_scan_1024(bool flag, int* s_warp, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+  const int in_warp = __popc(bal & lanemask_lt());
+  if (lane == 0) s_warp[warp] = __popc(bal);
+  __syncthreads();
+  if (warp == 0) {
+    int v = s_warp[lane];
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int n = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += n;
+    }
+    s_warp[lane] = incl - v;  // exclusive
+    if (lane == 31) s_warp[32] = incl;
+  }
+  __syncthreads();
+  const int pos = s_warp[warp] + in_warp;
+  *total = s_warp[32];
+  __syncthreads();
+  return pos;
+}
+
+// ---------------------------------------------------------------------------
+// k_sample_minibatch: one 1024-thread CTA.  Stratified random node
+// (network.cc:410-421): flag = randint(0,1); non-link stratum
+// (network.cc:274-349): source v and the first m valid new partners u in
+// candidate order (u != v, (v,u) not an edge, not held-out, not test); link
+// stratum (network.cc:355-407, max-source 1): all training edges of a random
+// v, redrawn while empty.  Candidates are examined in rounds of
+// need = m - count; within a round the first occurrence of each u wins
+// (atomicMin of its index in a hash), then an ordered block scan appends
+// them -- exactly the sequential scan of the oracle.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, Buffers b) {
+  __shared__ int s_warp[33];
+  __shared__ int s_flag, s_count;
+  __shared__ uint32_t s_step;
+  const int tid = threadIdx.x;
+  const Stream rs{m.seed, m.chain};
+  if (tid == 0) {
+    const uint32_t step = b.st->next_step;
+    b.st->step = step;
+    b.st->next_step = step + 1;
+    b.st->eps = eps_schedule(m.a, m.b, m.c, step);
+    int flag;
+    if (m.strategy == 0)
+      flag = (int)(rs.draw_u64(kTagMbFlag, 0, step, 0) % 2ull);
+    else
+      flag = (m.strategy == 1) ? 1 : 0;
+    s_flag = flag;
+    s_step = step;
+    s_count = 0;
+  }
+  __syncthreads();
+  const uint32_t step = s_step;
+  const int flag = s_flag;
+  int err = 0;
+  int rounds = 0;
+  if (flag == 0) {
+    const int mb = m.mini_batch_size;
+    const int32_t v = (int32_t)(rs.draw_u64(kTagMbNode, 0, step, 0) % (uint64_t)g.n);
+    for (uint32_t s = tid; s <= b.hmask; s += blockDim.x) {
+      b.htab_key[s] = 0xffffffffu;
+      b.htab_idx[s] = 0xffffffffu;
+    }
+    if (mb > m.max_edges || mb + 1 > m.max_nodes) err |= kErrCapacity;
+    if (tid == 0) b.nodes[0] = v;
+    __syncthreads();
+    int count = 0;
+    uint64_t t = 0;
+    const uint64_t cap = 64ull * (uint64_t)mb + 4096ull;
+    while (!err && count < mb) {
+      const int need = mb - count;
+      if (t + (uint64_t)need > cap) {
+        err |= kErrMinibatchCap;
+        break;
+      }
+      // pass A: validity and first-occurrence index per value
+      for (int c = tid; c < need; c += blockDim.x) {
+        const int32_t u = (int32_t)(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c) % (uint64_t)g.n);
+        const bool ok = (u != v) && !has_edge(g, v, u) && !is_excluded(g, v, u);
+        b.cand[c] = ok ? u : -1;
+        if (ok) {
+          uint32_t slot = hash32((uint32_t)u) & b.hmask;
+          for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
+            uint32_t prev = atomicCAS(b.htab_key + slot, 0xffffffffu, (uint32_t)u);
+            if (prev == 0xffffffffu || prev == (uint32_t)u) {
+              atomicMin(b.htab_idx + slot, (uint32_t)(t + (uint64_t)c));
+              break;
+            }
+            slot = (slot + 1) & b.hmask;
+          }
+        }
+      }
+      __syncthreads();
+      // pass B: ordered compaction of first occurrences
+      for (int base = 0; base < need; base += blockDim.x) {
+        const int c = base + tid;
+        int32_t u = -1;
+        bool acc = false;
+        if (c < need) {
+          u = b.cand[c];
+          if (u >= 0) {
+            uint32_t slot = hash32((uint32_t)u) & b.hmask;
+            for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
+              const uint32_t k = b.htab_key[slot];
+              if (k == (uint32_t)u) {
+                acc = (b.htab_idx[slot] == (uint32_t)(t + (uint64_t)c));
+                break;
+              }
+              if (k == 0xffffffffu) break;
+              slot = (slot + 1) & b.hmask;
+            }
+          }
+        }
+        int total;
+        const int pos = block_scan_1024(acc, s_warp, &total);
+        if (acc) {
+          const int e = count + pos;
+          b.nodes[e + 1] = u;
+          b.ea[e] = 0;
+          b.eb[e] = e + 1;
+          b.ey[e] = 0;
+        }
+        count += total;
+      }
+      t += (uint64_t)need;
+      ++rounds;
+      __syncthreads();
+    }
+    if (tid == 0) {
+      b.st->scale = m.nonlink_scale;
+      s_count = count;
+    }
+  } else {
+    int count = 0;
+    for (int attempt = 0; attempt < 4096 && count == 0 && !err; ++attempt) {
+      const int32_t v = (int32_t)(rs.draw_u64(kTagMbNode, 0, step, (uint64_t)attempt) % (uint64_t)g.n);
+      const int64_t r0 = g.row_ptr[v], deg = g.row_ptr[v + 1] - r0;
+      if (deg > m.max_edges || deg + 1 > m.max_nodes) {
+        err |= kErrCapacity;
+        break;
+      }
+      for (int64_t base = 0; base < deg; base += blockDim.x) {
+        const int64_t q = base + tid;
+        int32_t u = -1;
+        bool acc = false;
+        if (q < deg) {
+          u = g.col[r0 + q];
+          acc = !is_excluded(g, v, u);
+        }
+        int total;
+        const int pos = block_scan_1024(acc, s_warp, &total);
+        if (acc) {
+          const int e = count + pos;
+          b.nodes[e + 1] = u;
+          b.ea[e] = 0;
+          b.eb[e] = e + 1;
+          b.ey[e] = 1;
+        }
+        count += total;
+      }
+      if (count > 0 && tid == 0) b.nodes[0] = v;
+      rounds = attempt + 1;
+    }
+    if (count == 0 && !err) err |= kErrMinibatchCap;
+    if (tid == 0) {
+      b.st->scale = m.link_scale;
+      s_count = count;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    b.st->flag = flag;
+    b.st->n_edges = s_count;
+    b.st->n_nodes = err ? 0 : s_count + 1;
+    b.st->rounds = rounds;
+    if (err) atomicOr(&b.st->err, err);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_sample_neighbors: one warp per minibatch node.  n_out distinct ids j,
+// j != i, (i,j) neither held-out nor test (h:87-108); 32 candidates per
+// round, the first valid new ones in candidate order are kept; y_ij is the
+// graph membership the update needs (cc:279-283).
+// ---------------------------------------------------------------------------
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGraph g, Buffers b) {
+  extern __shared__ int32_t s_acc[];  // WARPS x n_out
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t* acc = s_acc + warp * m.n_out;
+  const int n_nodes = b.st->n_nodes;
+  const uint32_t step = b.st->step;
+  const Stream rs{m.seed, m.chain};
+  const uint64_t cap = 64ull * (uint64_t)m.n_out + 4096ull;
+  for (int slot = blockIdx.x * WARPS + warp; slot < n_nodes; slot += gridDim.x * WARPS) {
+    const int32_t i = b.nodes[slot];
+    int count = 0;
+    uint64_t t = 0;
+    while (count < m.n_out) {
+      if (t >= cap) {
+        if (lane == 0) atomicOr(&b.st->err, kErrNeighborCap);
+        break;
+      }
+      const int32_t j = (int32_t)(rs.draw_u64(kTagNbr, (uint32_t)i, step, t + lane) % (uint64_t)g.n);
+      bool ok = (j != i) && !is_excluded(g, i, j);
+      for (int q = 0; q < count && ok; ++q) ok = (acc[q] != j);
+      const uint32_t peers = __match_any_sync(0xffffffffu, j);
+      ok = ok && ((peers & lanemask_lt()) == 0);
+      const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+      const int pos = __popc(bal & lanemask_lt());
+      const int need = m.n_out - count;
+      if (ok && pos < need) {
+        const int idx = count + pos;
+        acc[idx] = j;
+        const uint32_t y = has_edge(g, i, j) ? 1u : 0u;
+        b.nbr[(int64_t)slot * m.n_out + idx] = (uint32_t)j | (y << 31);
+      }
+      count += min(__popc(bal), need);
+      t += 32;
+      __syncwarp();
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_update_phi: update_phi (cc:269-313) for NPB minibatch nodes per CTA,
+// SPLIT sub-groups of LPN lanes per node, each lane holding VPL 16-byte
+// vectors of a pi row.  Sub-group s takes neighbours s, s+SPLIT, ...
+//
+// Algebra (exact rewrite of the reference's per-k loop).  With
+// pi_ik = phi_ik / S, sigma_j = +1 for y=1 else -1, e_j = y ? eps : 1-eps,
+// bk = beta_k - epsilon and w_k = pi_ik * bk:
+//   probs_jk = pi_ik (sigma_j bk pi_jk + e_j)
+//   P_j      = sum_k probs_jk = sigma_j D_j + e_j s_i,
+//              D_j = sum_k w_k pi_jk,  s_i = sum_k pi_ik
+//   grad_k   = sum_j probs_jk / (P_j phi_ik) - 1/S
+//            = (bk A_k + B) / S,  A_k = sum_j (sigma_j / P_j) pi_jk,
+//              B = sum_j (e_j (1 - s_i) - sigma_j D_j) / P_j
+// so each neighbour row costs two FMAs per element (D_j, then A_k).
+// Epilogue: phi_ik <- |phi + eps/2 (alpha - phi + Nn grad) + sqrt(eps phi)
+// noise|, clamped to 1e-24; the new row is normalised into the staging
+// buffer (pi itself is written after all nodes, by k_commit_beta).
+// ---------------------------------------------------------------------------
+template <typename PiT, int LPN, int VPL, int SPLIT, int NPB>
+__global__ void __launch_bounds__(NPB * SPLIT * LPN)
+    k_update_phi(Model m, Buffers b) {
+  using TR = PiTraits<PiT>;
+  constexpr int EV = TR::kPerVec;
+  constexpr int EPL = VPL * EV;
+  constexpr int TPN = SPLIT * LPN;
+  extern __shared__ float s_dyn[];
+  float* s_A = s_dyn;                               // NPB x SPLIT x Kp
+  float* s_B = s_A + (size_t)NPB * SPLIT * m.Kp;    // NPB x SPLIT
+  float* s_red = s_B + NPB * SPLIT;                 // NPB x (TPN/32 or 1)
+
+  const int tid = threadIdx.x;
+  const int ln = tid / TPN;          // node within the CTA
+  const int r = tid - ln * TPN;      // thread within the node
+  const int sg = r / LPN;            // sub-group
+  const int l = r - sg * LPN;        // lane within the sub-group
+  const int warp_lane = tid & 31;
+  const uint32_t gmask = group_mask<LPN>(warp_lane);
+  const int n_nodes = b.st->n_nodes;
+  const uint32_t step = b.st->step;
+  const float eps_t = b.st->eps;
+  const int Kp = m.Kp, K = m.K;
+  const int nvec = Kp / EV;
+  const PiT* __restrict__ pi = reinterpret_cast<const PiT*>(b.pi);
+  const Stream rs{m.seed, m.chain};
+
+  for (int base = blockIdx.x * NPB; base < n_nodes; base += gridDim.x * NPB) {
+    const int slot = base + ln;
+    const bool active = slot < n_nodes;
+    float S = 0.f, s_i = 0.f, Bsum = 0.f;
+    if (active) {
+      const int32_t i = b.nodes[slot];
+      const float* phi_i = b.phi + (int64_t)i * Kp;
+      float w[EPL], A[EPL];
+      // phi row -> S
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = l + LPN * v;
+#pragma unroll
+        for (int e = 0; e < EV; ++e) {
+          const int k = vi * EV + e;
+          w[v * EV + e] = (vi < nvec) ? phi_i[k] : 0.f;
+          S += w[v * EV + e];
+        }
+      }
+#pragma unroll
+      for (int o = LPN / 2; o > 0; o >>= 1) S += __shfl_xor_sync(gmask, S, o);
+      // pi_i = phi_i / S, s_i = sum pi_i, w = pi_i * (beta - epsilon)
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = l + LPN * v;
+#pragma unroll
+        for (int e = 0; e < EV; ++e) {
+          const int k = vi * EV + e;
+          const float p = __fdiv_rn(w[v * EV + e], S);
+          s_i += p;
+          const float bk = (vi < nvec && k < K) ? (b.beta[k] - m.epsilon) : 0.f;
+          w[v * EV + e] = p * bk;
+          A[v * EV + e] = 0.f;
+        }
+      }
+#pragma unroll
+      for (int o = LPN / 2; o > 0; o >>= 1) s_i += __shfl_xor_sync(gmask, s_i, o);
+      const float one_m_si = 1.0f - s_i;
+      const uint32_t* nb = b.nbr + (int64_t)slot * m.n_out;
+
+      // neighbour loop, one row prefetched ahead
+      uint4 cur[VPL], nxt[VPL];
+      uint32_t wcur = 0, wnxt = 0;
+      int q = sg;
+      if (q < m.n_out) {
+        wcur = nb[q];
+        const PiT* row = pi + (int64_t)(wcur & 0x7fffffffu) * Kp;
+#pragma unroll
+        for (int v = 0; v < VPL; ++v) {
+          const int vi = l + LPN * v;
+          cur[v] = (vi < nvec) ? ldg_nc_v4(row + vi * EV) : make_uint4(0, 0, 0, 0);
+        }
+      }
+      for (; q < m.n_out; q += SPLIT) {
+        const int qn = q + SPLIT;
+        if (qn < m.n_out) {
+          wnxt = nb[qn];
+          const PiT* row = pi + (int64_t)(wnxt & 0x7fffffffu) * Kp;
+#pragma unroll
+          for (int v = 0; v < VPL; ++v) {
+            const int vi = l + LPN * v;
+            nxt[v] = (vi < nvec) ? ldg_nc_v4(row + vi * EV) : make_uint4(0, 0, 0, 0);
+          }
+        }
+        float x[EPL];
+#pragma unroll
+        for (int v = 0; v < VPL; ++v) TR::unpack(cur[v], x + v * EV);
+        float D = 0.f;
+#pragma unroll
+        for (int e = 0; e < EPL; ++e) D = fmaf(w[e], x[e], D);
+#pragma unroll
+        for (int o = LPN / 2; o > 0; o >>= 1) D += __shfl_xor_sync(gmask, D, o);
+        const bool y = (wcur >> 31) != 0;
+        const float sg_ = y ? 1.f : -1.f;
+        const float ej = y ? m.epsilon : 1.0f - m.epsilon;
+        const float P = fmaf(sg_, D, ej * s_i);
+        const float invP = __frcp_rn(P);
+        const float cj = sg_ * invP;
+        Bsum += (ej * one_m_si - sg_ * D) * invP;
+#pragma unroll
+        for (int e = 0; e < EPL; ++e) A[e] = fmaf(cj, x[e], A[e]);
+#pragma unroll
+        for (int v = 0; v < VPL; ++v) cur[v] = nxt[v];
+        wcur = wnxt;
+      }
+      // publish A and B of this sub-group
+      float* sA = s_A + ((size_t)ln * SPLIT + sg) * Kp;
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = l + LPN * v;
+        if (vi < nvec) {
+#pragma unroll
+          for (int e = 0; e < EV; ++e) sA[vi * EV + e] = A[v * EV + e];
+        }
+      }
+      if (l == 0) s_B[ln * SPLIT + sg] = Bsum;
+    }
+    __syncthreads();
+    // epilogue: TPN threads per node, element k = r + TPN * q
+    // each sub-group covers the whole row: Kp <= LPN * EPL = TPN * EPL / SPLIT
+    constexpr int NQ = (EPL + SPLIT - 1) / SPLIT;
+    float pnew[NQ];
+    float Snew = 0.f;
+    int32_t i = 0;
+    if (active) {
+      i = b.nodes[slot];
+      float Bt = 0.f;
+#pragma unroll
+      for (int s = 0; s < SPLIT; ++s) Bt += s_B[ln * SPLIT + s];
+      float* phi_i = b.phi + (int64_t)i * Kp;
+      const float invS = 1.0f / S;
+      const float half_eps = eps_t / 2.0f;
+#pragma unroll
+      for (int qq = 0; qq < NQ; ++qq) {
+        const int k = r + TPN * qq;
+        float val = 0.f;
+        if (k < K) {
+          float Ak = 0.f;
+#pragma unroll
+          for (int s = 0; s < SPLIT; ++s) Ak += s_A[((size_t)ln * SPLIT + s) * Kp + k];
+          const float bk = b.beta[k] - m.epsilon;
+          const float grad = (bk * Ak + Bt) * invS;
+          const float noise = b.fed_phi_noise
+                                  ? b.fed_phi_noise[(int64_t)slot * K + k]
+                                  : normal_draw(rs, kTagPhiNoise, (uint32_t)i, step, (uint64_t)k);
+          const float ph = phi_i[k];
+          val = fabsf((ph + half_eps * (m.alpha - ph + m.Nn * grad)) + sqrtf(eps_t * ph) * noise);
+          if (val < 1.0e-24f) val = 1.0e-24f;
+          phi_i[k] = val;
+        }
+        pnew[qq] = val;
+        Snew += val;
+      }
+    }
+    // sum of the new row over the node's TPN threads
+    if constexpr (TPN <= 32) {
+#pragma unroll
+      for (int o = TPN / 2; o > 0; o >>= 1) Snew += __shfl_xor_sync(group_mask<TPN>(warp_lane), Snew, o);
+    } else {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) Snew += __shfl_xor_sync(0xffffffffu, Snew, o);
+      if (warp_lane == 0) s_red[ln * (TPN / 32) + (r >> 5)] = Snew;
+      __syncthreads();
+      Snew = 0.f;
+#pragma unroll
+      for (int w2 = 0; w2 < TPN / 32; ++w2) Snew += s_red[ln * (TPN / 32) + w2];
+    }
+    if (active) {
+      float* st = b.stage + (int64_t)slot * Kp;
+#pragma unroll
+      for (int qq = 0; qq < NQ; ++qq) {
+        const int k = r + TPN * qq;
+        if (k < Kp) st[k] = (k < K) ? __fdiv_rn(pnew[qq], Snew) : 0.f;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_commit_beta: blocks [0, ncommit) copy the staged rows into pi (the
+// reference's update_pi loop, cc:162-166); blocks [ncommit, ncommit+nbb)
+// evaluate update_beta's per-edge terms (cc:212-240) on the staged (new) pi
+// and reduce them per block.  With f_k = pi_ak pi_bk, P_e = sum_k
+// (y ? beta_k : 1-beta_k) f_k + (y ? eps : 1-eps)(1 - sum_k f_k) the
+// gradient only needs R_yk = sum_{e: y_e = y} f_ek / P_e (k_theta applies the
+// theta factors), accumulated per warp in registers, then per block.
+// ---------------------------------------------------------------------------
+template <typename PiT, int KQ>
+__global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int ncommit) {
+  using TR = PiTraits<PiT>;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int Kp = m.Kp, K = m.K;
+  if ((int)blockIdx.x < ncommit) {
+    const int n_nodes = b.st->n_nodes;
+    constexpr int EV = TR::kPerVec;
+    PiT* pi = reinterpret_cast<PiT*>(b.pi);
+    const int nvec = Kp / EV;
+    for (int slot = blockIdx.x * 4 + warp; slot < n_nodes; slot += ncommit * 4) {
+      const int32_t i = b.nodes[slot];
+      const float* src = b.stage + (int64_t)slot * Kp;
+      PiT* dst = pi + (int64_t)i * Kp;
+      for (int vi = lane; vi < nvec; vi += 32) {
+        float x[EV];
+#pragma unroll
+        for (int e = 0; e < EV; ++e) x[e] = src[vi * EV + e];
+        *reinterpret_cast<uint4*>(dst + vi * EV) = TR::pack(x);
+      }
+    }
+    return;
+  }
+  __shared__ float s_part[4][2][KQ * 128];
+  const int bb = blockIdx.x - ncommit;
+  const int n_edges = b.st->n_edges;
+  float R0[KQ * 4], R1[KQ * 4], bt[KQ * 4];
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int k = q * 128 + lane * 4 + e;
+      R0[q * 4 + e] = 0.f;
+      R1[q * 4 + e] = 0.f;
+      bt[q * 4 + e] = (k < K) ? b.beta[k] : 0.f;
+    }
+  for (int ed = bb * 4 + warp; ed < n_edges; ed += m.nbb * 4) {
+    const float* pa = b.stage + (int64_t)b.ea[ed] * Kp;
+    const float* pb = b.stage + (int64_t)b.eb[ed] * Kp;
+    const bool y = b.ey[ed] != 0;
+    float f[KQ * 4];
+    float fsum = 0.f, psum = 0.f;
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int k0 = q * 128 + lane * 4;
+      float4 xa = make_float4(0, 0, 0, 0), xb = make_float4(0, 0, 0, 0);
+      if (k0 < Kp) {
+        xa = *reinterpret_cast<const float4*>(pa + k0);
+        xb = *reinterpret_cast<const float4*>(pb + k0);
+      }
+      f[q * 4 + 0] = xa.x * xb.x;
+      f[q * 4 + 1] = xa.y * xb.y;
+      f[q * 4 + 2] = xa.z * xb.z;
+      f[q * 4 + 3] = xa.w * xb.w;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float fk = f[q * 4 + e];
+        fsum += fk;
+        psum += (y ? bt[q * 4 + e] : (k0 + e < K ? 1.0f - bt[q * 4 + e] : 0.f)) * fk;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
+      psum += __shfl_xor_sync(0xffffffffu, psum, o);
+    }
+    const float prob0 = (y ? m.epsilon : 1.0f - m.epsilon) * (1.0f - fsum);
+    const float invP = 1.0f / (psum + prob0);
+    if (y) {
+#pragma unroll
+      for (int e = 0; e < KQ * 4; ++e) R1[e] = fmaf(f[e], invP, R1[e]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < KQ * 4; ++e) R0[e] = fmaf(f[e], invP, R0[e]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      s_part[warp][0][q * 128 + lane * 4 + e] = R0[q * 4 + e];
+      s_part[warp][1][q * 128 + lane * 4 + e] = R1[q * 4 + e];
+    }
+  __syncthreads();
+  float* out = b.beta_part + (int64_t)bb * 2 * Kp;
+  for (int k = threadIdx.x; k < Kp; k += 128) {
+    out[k] = s_part[0][0][k] + s_part[1][0][k] + s_part[2][0][k] + s_part[3][0][k];
+    out[Kp + k] = s_part[0][1][k] + s_part[1][1][k] + s_part[2][1][k] + s_part[3][1][k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_theta: theta step of update_beta (cc:241-266) in FP64.  With the block
+// sums R0_k, R1_k and beta_k the gradients of cc:236-239 are
+//   G_k0 = beta R1 (0 - 1/ts) + (1-beta) R0 (1/theta_k0 - 1/ts)
+//   G_k1 = beta R1 (1/theta_k1 - 1/ts) + (1-beta) R0 (0 - 1/ts)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_theta(Model m, Buffers b) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m.K) return;
+  const uint32_t step = b.st->step;
+  const double eps_t = (double)b.st->eps;
+  const double scale = (double)b.st->scale;
+  const int Kp = m.Kp;
+  double R0 = 0.0, R1 = 0.0;
+  for (int bb = 0; bb < m.nbb; ++bb) {
+    R0 += (double)b.beta_part[(int64_t)bb * 2 * Kp + k];
+    R1 += (double)b.beta_part[(int64_t)bb * 2 * Kp + Kp + k];
+  }
+  const double th0 = b.theta[2 * k], th1 = b.theta[2 * k + 1];
+  const double ts_inv = 1.0 / (th0 + th1);
+  const double bt = (double)b.beta[k];
+  const double G0 = bt * R1 * (-ts_inv) + (1.0 - bt) * R0 * (1.0 / th0 - ts_inv);
+  const double G1 = bt * R1 * (1.0 / th1 - ts_inv) + (1.0 - bt) * R0 * (-ts_inv);
+  const Stream rs{m.seed, m.chain};
+  double n0, n1;
+  if (b.fed_theta_noise) {
+    n0 = b.fed_theta_noise[2 * k];
+    n1 = b.fed_theta_noise[2 * k + 1];
+  } else {
+    n0 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k);
+    n1 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k + 1);
+  }
+  double t0 = fabs(th0 + eps_t / 2.0 * ((double)m.eta0 - th0 + scale * G0) + sqrt(eps_t * th0) * n0);
+  double t1 = fabs(th1 + eps_t / 2.0 * ((double)m.eta1 - th1 + scale * G1) + sqrt(eps_t * th1) * n1);
+  if (t0 < 1.0e-24) t0 = 1.0e-24;
+  if (t1 < 1.0e-24) t1 = 1.0e-24;
+  b.theta[2 * k] = t0;
+  b.theta[2 * k + 1] = t1;
+  b.beta[k] = (float)(t1 / (t0 + t1));
+}
+
+// ---------------------------------------------------------------------------
+// Held-out perplexity (learner.cc:138-183, learner.h:100-139): LPN lanes per
+// held-out edge; running average per edge in FP32 as the reference; the log
+// sum in FP64 with Kahan compensation, block partials, then k_ppx_final.
+// ---------------------------------------------------------------------------
+template <typename PiT, int LPN, int VPL>
+__global__ void __launch_bounds__(256) k_perplexity(Model m, const PiT* __restrict__ pi,
+                                                    const float* __restrict__ beta,
+                                                    const int32_t* __restrict__ ha,
+                                                    const int32_t* __restrict__ hb,
+                                                    const uint8_t* __restrict__ hy, int64_t H,
+                                                    float* __restrict__ ppx, float count,
+                                                    double* __restrict__ part) {
+  using TR = PiTraits<PiT>;
+  constexpr int EV = TR::kPerVec;
+  constexpr int EPL = VPL * EV;
+  constexpr int GPB = 256 / LPN;
+  const int tid = threadIdx.x, grp = tid / LPN, l = tid % LPN, lane = tid & 31;
+  const uint32_t gmask = group_mask<LPN>(lane);
+  const int Kp = m.Kp, K = m.K, nvec = Kp / EV;
+  float bt[EPL];
+#pragma unroll
+  for (int v = 0; v < VPL; ++v)
+#pragma unroll
+    for (int e = 0; e < EV; ++e) {
+      const int k = (l + LPN * v) * EV + e;
+      bt[v * EV + e] = (k < K) ? beta[k] : 0.f;
+    }
+  double sum = 0.0, comp = 0.0;
+  for (int64_t ed = (int64_t)blockIdx.x * GPB + grp; ed < H; ed += (int64_t)gridDim.x * GPB) {
+    const PiT* ra = pi + (int64_t)ha[ed] * Kp;
+    const PiT* rb = pi + (int64_t)hb[ed] * Kp;
+    const bool y = hy[ed] != 0;
+    float s = 0.f, fs = 0.f;
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) {
+      const int vi = l + LPN * v;
+      if (vi < nvec) {
+        float xa[EV], xb[EV];
+        TR::unpack(ldg_nc_v4(ra + vi * EV), xa);
+        TR::unpack(ldg_nc_v4(rb + vi * EV), xb);
+#pragma unroll
+        for (int e = 0; e < EV; ++e) {
+          const float f = xa[e] * xb[e];
+          fs += f;
+          s += f * (y ? bt[v * EV + e] : (vi * EV + e < K ? 1.0f - bt[v * EV + e] : 0.f));
+        }
+      }
+    }
+#pragma unroll
+    for (int o = LPN / 2; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(gmask, s, o);
+      fs += __shfl_xor_sync(gmask, fs, o);
+    }
+    if (l == 0) {
+      if (!y) s += (1.0f - fs) * (1.0f - m.epsilon);
+      if (s < 1.0e-30f) s = 1.0e-30f;
+      const float avg = (ppx[ed] * (count - 1.0f) + s) / count;
+      ppx[ed] = avg;
+      const double term = log((double)avg) - comp;
+      const double tsum = sum + term;
+      comp = (tsum - sum) - term;
+      sum = tsum;
+    }
+  }
+  // block reduction, compensated pairwise in fixed order
+  __shared__ double s_sum[256], s_comp[256];
+  s_sum[tid] = sum;
+  s_comp[tid] = comp;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0, c = 0.0;
+    for (int q = 0; q < 256; q += LPN) {
+      const double term = (s_sum[q] - s_comp[q]) - c;
+      const double ts = t + term;
+      c = (ts - t) - term;
+      t = ts;
+    }
+    part[2 * blockIdx.x] = t;
+    part[2 * blockIdx.x + 1] = c;
+  }
+}
+
+__global__ void k_ppx_final(const double* part, int nblk, int64_t H, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t = 0.0, c = 0.0;
+  for (int q = 0; q < nblk; ++q) {
+    const double term = (part[2 * q] - part[2 * q + 1]) - c;
+    const double ts = t + term;
+    c = (ts - t) - term;
+    t = ts;
+  }
+  out[0] = H ? -(t / (double)H) : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// init: phi ~ Gamma(1,1) (cc:66), row normalisation into pi (cc:75)
+// ---------------------------------------------------------------------------
+__global__ void k_init_phi(Model m, float* phi, double shape, double scale, int32_t* err) {
+  const Stream rs{m.seed, m.chain};
+  const int64_t total = m.N * (int64_t)m.Kp;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = x / m.Kp;
+    const int k = (int)(x - v * m.Kp);
+    phi[x] = (k < m.K) ? (float)gamma_draw(rs, kTagPhiInit, (uint32_t)v, (uint64_t)k, shape, scale, err)
+                       : 0.f;
+  }
+}
+
+// np::row_normalize (np.h:63-75): one warp per row, sum in FP32.
+template <typename PiT>
+__global__ void k_normalize_rows(Model m, const float* phi, PiT* pi) {
+  using TR = PiTraits<PiT>;
+  constexpr int EV = TR::kPerVec;
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int Kp = m.Kp, nvec = Kp / EV;
+  for (int64_t v = w0; v < m.N; v += nw) {
+    const float* src = phi + v * Kp;
+    float s = 0.f;
+    for (int k = lane; k < Kp; k += 32) s += src[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    PiT* dst = pi + v * Kp;
+    for (int vi = lane; vi < nvec; vi += 32) {
+      float x[EV];
+#pragma unroll
+      for (int e = 0; e < EV; ++e) x[e] = __fdiv_rn(src[vi * EV + e], s);
+      *reinterpret_cast<uint4*>(dst + vi * EV) = TR::pack(x);
+    }
+  }
+}
+
+}  // namespace ammsb

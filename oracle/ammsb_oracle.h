@@ -1,0 +1,196 @@
+/*
+ * ammsb_oracle.h -- CPU oracle for the a-MMSB SG-MCMC hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the mcmc_for_ammsb_gb300
+ * package, its CUDA library, its C-ABI) may link, load or call this code.
+ * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline /
+ * reference legs use it, as the checker.
+ *
+ * Two kinds of functions live here:
+ *   1. Literal restatements of the reference sampler's arithmetic
+ *      (mcmc_sampler_stochastic.cc update_phi / update_beta, learner.h
+ *      cal_edge_likelihood, learner.cc cal_perplexity), in the reference's
+ *      own operation order, in float (the reference's default Float) and in
+ *      double (for error statements).
+ *   2. The sampling specification of this project: the reference's minibatch
+ *      and neighbour semantics (network.cc:274-421, mcmc_sampler_stochastic.h
+ *      :87-108) driven by a counter-based Philox4x32-10 stream instead of the
+ *      reference's sequential xorshift128+ (random.cc:136-142).  The CUDA
+ *      sampler must reproduce these draws bit for bit.
+ */
+#ifndef AMMSB_ORACLE_H_
+#define AMMSB_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Philox4x32-10 (Salmon et al., SC'11) -------------------------------- */
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                          uint32_t out[4]);
+
+/* Stream tags (counter word 3, low byte). */
+enum {
+  OR_P_MB_FLAG = 1,
+  OR_P_MB_NODE = 2,
+  OR_P_MB_CAND = 3,
+  OR_P_NBR = 4,
+  OR_P_PHI_NOISE = 5,
+  OR_P_THETA_NOISE = 6,
+  OR_P_PHI_INIT = 7,
+  OR_P_THETA_INIT = 8
+};
+
+/* 64-bit uniform draw #t of stream (tag, entity, step): two 32-bit words of
+ * Philox block t/2, half t%2. */
+uint64_t oracle_draw_u64(uint32_t seed, uint32_t chain, uint32_t tag,
+                         uint32_t entity, uint32_t step, uint64_t t);
+
+/* Standard normals of stream (tag, entity, step), element idx: Box-Muller on
+ * 24-bit uniforms, four normals per Philox block. */
+float oracle_normal(uint32_t seed, uint32_t chain, uint32_t tag,
+                    uint32_t entity, uint32_t step, uint64_t idx);
+
+/* Marsaglia-Tsang gamma(shape, scale) draw for element (entity, idx). */
+double oracle_gamma(uint32_t seed, uint32_t chain, uint32_t tag,
+                    uint32_t entity, uint64_t idx, double shape, double scale);
+
+/* ---- graph queries --------------------------------------------------------*/
+typedef struct {
+  int64_t n;               /* vertices */
+  const int64_t *row_ptr;  /* n+1 */
+  const int32_t *col;      /* row_ptr[n], each row sorted ascending */
+  const uint64_t *excl;    /* sorted keys (min<<32|max) of held-out + test */
+  int64_t n_excl;
+} oracle_graph;
+
+int oracle_has_edge(const oracle_graph *g, int32_t a, int32_t b);
+int oracle_is_excluded(const oracle_graph *g, int32_t a, int32_t b);
+
+/* ---- sampling spec (Philox-driven restatement of the reference) ----------*/
+typedef struct {
+  int32_t flag;       /* 0: non-link stratum, 1: link stratum */
+  int32_t n_edges;
+  int32_t n_nodes;
+  float scale;
+  int32_t rounds;     /* non-link rounds or link attempts used */
+} oracle_mb_info;
+
+/* stratified-random-node (strategy 0), -links (1), -nonlinks (2).
+ * edge_a/edge_b/edge_y get n_edges entries (slot of endpoint in nodes[]),
+ * nodes gets n_nodes vertex ids; capacities are max_edges / max_nodes.
+ * Returns 0 on success, negative on a capped loop or capacity overflow. */
+int oracle_sample_minibatch(const oracle_graph *g, int strategy,
+                            int64_t mini_batch_size, int64_t num_total_edges,
+                            uint32_t seed, uint32_t chain, uint32_t step,
+                            int32_t *edge_a, int32_t *edge_b, uint8_t *edge_y,
+                            int32_t max_edges, int32_t *nodes,
+                            int32_t max_nodes, oracle_mb_info *info);
+
+/* n_out distinct neighbours of node (n_out = num_node_sample + 1), each
+ * != node and not a held-out/test pair; y[t] = graph membership.
+ * Returns number of candidate draws used, negative on cap. */
+int64_t oracle_sample_neighbors(const oracle_graph *g, int32_t node,
+                                int32_t n_out, uint32_t seed, uint32_t chain,
+                                uint32_t step, int32_t *out, uint8_t *y);
+
+/* Scale factors of the two strata (network.cc:341-342, 385-390). */
+float oracle_nonlink_scale(int64_t N, int64_t m, int64_t num_total_edges);
+
+/* eps_t = a (1 + t/b)^-c (mcmc_sampler_stochastic.h:112-115), in double then
+ * rounded to float. */
+float oracle_eps_t(double a, double b, double c, uint64_t step);
+
+/* ---- hot-path arithmetic, literal restatements --------------------------*/
+/* update_phi for one node (mcmc_sampler_stochastic.cc:269-313).
+ * pi: N x K row-major (stride K); phi_i: K (updated in place);
+ * nbrs: n_nbrs ids in iteration order; y: per neighbour; noise: K. */
+void oracle_update_phi_f32(int32_t K, const float *pi, float *phi_i,
+                           int32_t i, const int32_t *nbrs, const uint8_t *y,
+                           int32_t n_nbrs, const float *beta, float alpha,
+                           float epsilon, float eps_t, int64_t N,
+                           int64_t num_node_sample, const float *noise);
+void oracle_update_phi_f64(int32_t K, const double *pi, double *phi_i,
+                           int32_t i, const int32_t *nbrs, const uint8_t *y,
+                           int32_t n_nbrs, const double *beta, double alpha,
+                           double epsilon, double eps_t, int64_t N,
+                           int64_t num_node_sample, const double *noise);
+
+/* The update_phi gradient alone (grads[k] before the SGRLD step). */
+void oracle_phi_grad_f64(int32_t K, const double *pi, const double *phi_i,
+                         int32_t i, const int32_t *nbrs, const uint8_t *y,
+                         int32_t n_nbrs, const double *beta, double epsilon,
+                         double *grads);
+
+/* np::normalize (np.h:39-56) */
+void oracle_normalize_f32(int32_t K, const float *phi_i, float *pi_i);
+void oracle_normalize_f64(int32_t K, const double *phi_i, double *pi_i);
+
+/* update_beta (mcmc_sampler_stochastic.cc:200-267): gradient over the
+ * minibatch edges (ea, eb vertex ids, ey), theta step with noise K x 2,
+ * beta = theta1 / (theta0 + theta1).  grads_out (K x 2) optional. */
+void oracle_update_beta_f32(int32_t K, const float *pi, const int32_t *ea,
+                            const int32_t *eb, const uint8_t *ey,
+                            int32_t n_edges, float *theta, float *beta,
+                            const float *eta, float epsilon, float eps_t,
+                            float scale, const float *noise, float *grads_out);
+void oracle_update_beta_f64(int32_t K, const double *pi, const int32_t *ea,
+                            const int32_t *eb, const uint8_t *ey,
+                            int32_t n_edges, double *theta, double *beta,
+                            const double *eta, double epsilon, double eps_t,
+                            double scale, const double *noise,
+                            double *grads_out);
+
+/* cal_edge_likelihood (learner.h:100-139) */
+float oracle_edge_likelihood_f32(int32_t K, const float *pa, const float *pb,
+                                 int y, const float *beta, float epsilon);
+double oracle_edge_likelihood_f64(int32_t K, const double *pa,
+                                  const double *pb, int y, const double *beta,
+                                  double epsilon);
+
+/* cal_perplexity (learner.cc:138-183) over held-out edges (ha, hb, hy) with
+ * running averages ppx (updated) and average_count (caller increments).
+ * f32: the reference's float accumulation.  f64acc: float likelihoods and
+ * float running average (the device's storage types) with the log-sum in
+ * double -- the semantics of the CUDA perplexity kernel. */
+float oracle_perplexity_f32(int32_t K, const float *pi, const int32_t *ha,
+                            const int32_t *hb, const uint8_t *hy, int64_t H,
+                            const float *beta, float epsilon, float *ppx,
+                            uint64_t average_count);
+double oracle_perplexity_f64acc(int32_t K, const float *pi, const int32_t *ha,
+                                const int32_t *hb, const uint8_t *hy,
+                                int64_t H, const float *beta, float epsilon,
+                                float *ppx, uint64_t average_count);
+double oracle_perplexity_f64(int32_t K, const double *pi, const int32_t *ha,
+                             const int32_t *hb, const uint8_t *hy, int64_t H,
+                             const double *beta, double epsilon, double *ppx,
+                             uint64_t average_count);
+
+/* ---- whole iteration ---------------------------------------------------*/
+typedef struct {
+  int32_t K;
+  int64_t N;
+  int64_t num_total_edges;
+  int32_t strategy;
+  int64_t mini_batch_size;
+  int64_t num_node_sample;
+  float alpha, epsilon, eta0, eta1;
+  double a, b, c;
+  uint32_t seed, chain;
+} oracle_params;
+
+/* One SG-MCMC iteration at `step` (draws from the Philox spec), float
+ * arithmetic in the reference's order: minibatch, neighbours, update_phi
+ * (Jacobi: all reads see the old pi), pi normalisation, update_beta.
+ * pi/phi: N x K; theta: K x 2 (float, as the reference); beta: K.
+ * Returns 0 or a negative sampling error. */
+int oracle_step_f32(const oracle_params *p, const oracle_graph *g,
+                    uint32_t step, float *pi, float *phi, float *theta,
+                    float *beta, oracle_mb_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

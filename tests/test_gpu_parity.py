@@ -1,0 +1,358 @@
+"""GPU parity tests: the CUDA path through the C ABI against the CPU oracle.
+
+Tolerances (written here, used below):
+  * sampling (flag, scale, minibatch edges, nodes, neighbour ids, y): exact;
+  * one fed phi/theta step, FP32 pi: 1e-5 relative against the oracle's
+    literal float restatement of update_phi / update_beta;
+  * the same step against the FP64 oracle: 1e-4 relative (stated error of
+    the float paths; the reference itself is float);
+  * perplexity: 1e-5 relative (device uses a compensated FP64 log-sum);
+  * trajectories: held-out perplexity within 1% at every checkpoint.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mcmc_for_ammsb_gb300 import MCMCSamplerStochastic, Network, Options, _native, workloads
+
+pytestmark = pytest.mark.gpu
+
+RTOL_STEP = 1e-5
+RTOL_F64 = 1e-4
+RTOL_PPX = 1e-5
+
+
+def rel_err(a, b, floor=1e-30):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if a.size else 0.0
+
+
+def random_state(N, K, seed=0, shape=1.0):
+    rng = np.random.default_rng(seed)
+    phi = rng.gamma(shape, 1.0 / shape if shape > 1 else 1.0, (N, K)).astype(np.float32)
+    phi = np.maximum(phi, np.float32(1e-6))
+    theta = rng.gamma(1.0, 1.0, (K, 2)).astype(np.float64) + 0.05
+    return phi, theta
+
+
+def make_sampler(net, dtype=_native.PI_F32, **kw):
+    o = dict(K=32, num_node_sample=32, a=0.01, b=1024.0, c=0.55, random_seed=42)
+    o.update(kw)
+    opts = Options(pi_dtype=dtype, **o)
+    return MCMCSamplerStochastic(opts, net).create(), opts
+
+
+@pytest.fixture(scope="module")
+def small(native_lib):
+    return workloads.build("small")
+
+
+@pytest.fixture(scope="module")
+def sparse_net(native_lib):
+    """A graph with many isolated vertices: the link stratum must redraw."""
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, 300, 400)
+    b = rng.integers(0, 300, 400)
+    net = Network.from_edges(1200, a, b)
+    net.make_held_out(0.05, seed=1)
+    return net
+
+
+# ---------------------------------------------------------------------------
+# sampling: bit-exact against the oracle's Philox specification
+# ---------------------------------------------------------------------------
+def check_sampling(s, net, opts, steps):
+    og = oracle.OracleGraph(net)
+    m = s.resolved.mini_batch_size
+    n_out = s.num_node_sample + 1
+    for _ in range(steps):
+        step = s.step_count
+        s.step(1)
+        got = s.last_minibatch()
+        want = oracle.sample_minibatch(og, opts.strategy, m, net.num_total_edges,
+                                       opts.random_seed, opts.chain, step, s.max_edges)
+        assert got["flag"] == want["flag"]
+        assert got["scale"] == pytest.approx(want["scale"], rel=0, abs=0)
+        for k in ("edge_a", "edge_b", "edge_y", "nodes"):
+            assert np.array_equal(got[k], want[k]), k
+        for r, node in enumerate(want["nodes"]):
+            nb, y = oracle.sample_neighbors(og, int(node), n_out, opts.random_seed, opts.chain,
+                                            step)
+            assert np.array_equal(got["nbrs"][r], nb), (step, r)
+            assert np.array_equal(got["nbr_y"][r], y), (step, r)
+
+
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+@pytest.mark.parametrize("strategy", [0, 1, 2])
+def test_sampling_bit_exact(small, dtype, strategy):
+    net, _ = small
+    s, opts = make_sampler(net, dtype, strategy=strategy)
+    phi, theta = random_state(net.N, 32)
+    s.set_state(phi, theta)
+    check_sampling(s, net, opts, steps=6)
+    s.close()
+
+
+def test_sampling_link_stratum_redraws_empty(sparse_net):
+    s, opts = make_sampler(sparse_net, strategy=1, K=16, num_node_sample=8, mini_batch_size=50)
+    s.set_state(*random_state(sparse_net.N, 16))
+    check_sampling(s, sparse_net, opts, steps=10)
+    s.close()
+
+
+def test_sampling_small_population_collisions(native_lib):
+    """N small relative to the draws: many duplicate candidates."""
+    rng = np.random.default_rng(9)
+    net = Network.from_edges(80, rng.integers(0, 80, 200), rng.integers(0, 80, 200))
+    net.make_held_out(0.1, seed=2)
+    s, opts = make_sampler(net, K=8, num_node_sample=40, mini_batch_size=30, strategy=0)
+    s.set_state(*random_state(net.N, 8))
+    check_sampling(s, net, opts, steps=8)
+    s.close()
+
+
+# ---------------------------------------------------------------------------
+# one fed step: update_phi + pi + update_beta against the literal oracle
+# ---------------------------------------------------------------------------
+def fed_inputs(net, s, opts, step, seed=0):
+    og = oracle.OracleGraph(net)
+    mb = oracle.sample_minibatch(og, 0, s.resolved.mini_batch_size, net.num_total_edges,
+                                 opts.random_seed, 0, step, s.max_edges)
+    n_out = s.num_node_sample + 1
+    nbrs = np.zeros((len(mb["nodes"]), n_out), np.int32)
+    nby = np.zeros_like(nbrs, dtype=np.uint8)
+    for r, node in enumerate(mb["nodes"]):
+        nbrs[r], nby[r] = oracle.sample_neighbors(og, int(node), n_out, opts.random_seed, 0, step)
+    rng = np.random.default_rng(seed)
+    pn = rng.standard_normal((len(mb["nodes"]), s.K)).astype(np.float32)
+    tn = rng.standard_normal((s.K, 2)).astype(np.float32)
+    return mb, nbrs, nby, pn, tn
+
+
+def oracle_fed_step(net, opts, resolved, phi, theta, mb, nbrs, nby, pn, tn, step, dtype):
+    K = phi.shape[1]
+    phi = phi.astype(dtype)
+    pi = oracle.normalize(phi, dtype)
+    th = theta.astype(dtype)
+    beta = (th[:, 1] / (th[:, 0] + th[:, 1])).astype(dtype)
+    eps = oracle.eps_t(resolved.a, resolved.b, resolved.c, step)
+    new_phi = phi.copy()
+    for r, node in enumerate(mb["nodes"]):
+        new_phi[node] = oracle.update_phi(K, pi, phi[node], int(node), nbrs[r], nby[r], beta,
+                                          resolved.alpha, resolved.epsilon, eps, net.N,
+                                          resolved.num_node_sample, pn[r], dtype)
+    new_pi = pi.copy()
+    idx = mb["nodes"]
+    new_pi[idx] = oracle.normalize(new_phi[idx], dtype)
+    ea = mb["nodes"][mb["edge_a"]]
+    eb = mb["nodes"][mb["edge_b"]]
+    eta = np.array([resolved.eta0, resolved.eta1])
+    th2, bt2, grads = oracle.update_beta(K, new_pi, ea, eb, mb["edge_y"], th, beta, eta,
+                                         resolved.epsilon, eps, mb["scale"], tn, dtype)
+    return new_phi, new_pi, th2, bt2
+
+
+@pytest.mark.parametrize("K", [32, 20])
+@pytest.mark.parametrize("step", [1, 37])
+def test_fed_step_matches_oracle_f32(small, K, step):
+    net, _ = small
+    s, opts = make_sampler(net, K=K)
+    phi, theta = random_state(net.N, K, seed=step)
+    s.set_state(phi, theta)
+    mb, nbrs, nby, pn, tn = fed_inputs(net, s, opts, step)
+    s.step_fed(step, np.stack([mb["edge_a"], mb["edge_b"]], 1), mb["edge_y"], mb["scale"],
+               mb["nodes"], nbrs, nby, pn, tn)
+    want_phi, want_pi, want_th, want_bt = oracle_fed_step(net, opts, s.resolved, phi, theta, mb,
+                                                          nbrs, nby, pn, tn, step, np.float32)
+    idx = mb["nodes"]
+    assert rel_err(s.phi[idx], want_phi[idx]) < RTOL_STEP
+    assert rel_err(s.pi[idx], want_pi[idx]) < RTOL_STEP
+    untouched = np.setdiff1d(np.arange(net.N), idx)
+    assert np.array_equal(s.phi[untouched], phi[untouched])
+    assert rel_err(s.theta, want_th) < RTOL_STEP
+    assert rel_err(s.beta, want_bt) < RTOL_STEP
+    # against FP64: the stated error of the float path
+    f_phi, f_pi, f_th, f_bt = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby,
+                                              pn, tn, step, np.float64)
+    assert rel_err(s.phi[idx], f_phi[idx]) < RTOL_F64
+    assert rel_err(s.theta, f_th) < RTOL_F64
+    s.close()
+
+
+def test_fed_step_link_stratum(small):
+    """A link-stratum (y = 1) minibatch through the fed path."""
+    net, _ = small
+    s, opts = make_sampler(net, strategy=1)
+    phi, theta = random_state(net.N, 32, seed=3)
+    s.set_state(phi, theta)
+    og = oracle.OracleGraph(net)
+    mb = oracle.sample_minibatch(og, 1, s.resolved.mini_batch_size, net.num_total_edges,
+                                 opts.random_seed, 0, 5, s.max_edges)
+    assert mb["flag"] == 1 and mb["edge_y"].all()
+    n_out = s.num_node_sample + 1
+    nbrs = np.zeros((len(mb["nodes"]), n_out), np.int32)
+    nby = np.zeros_like(nbrs, dtype=np.uint8)
+    for r, node in enumerate(mb["nodes"]):
+        nbrs[r], nby[r] = oracle.sample_neighbors(og, int(node), n_out, 42, 0, 5)
+    rng = np.random.default_rng(1)
+    pn = rng.standard_normal((len(mb["nodes"]), 32)).astype(np.float32)
+    tn = rng.standard_normal((32, 2)).astype(np.float32)
+    s.step_fed(5, np.stack([mb["edge_a"], mb["edge_b"]], 1), mb["edge_y"], mb["scale"],
+               mb["nodes"], nbrs, nby, pn, tn)
+    want_phi, want_pi, want_th, want_bt = oracle_fed_step(net, opts, s.resolved, phi, theta, mb,
+                                                          nbrs, nby, pn, tn, 5, np.float32)
+    assert rel_err(s.phi[mb["nodes"]], want_phi[mb["nodes"]]) < RTOL_STEP
+    assert rel_err(s.theta, want_th) < RTOL_STEP
+    s.close()
+
+
+def test_fed_step_k1024_bf16_runs(native_lib):
+    """Large-K row kernels (split sub-groups, 4 vectors per lane)."""
+    net = Network.synthetic(n=3000, k_true=30, intra_degree=6.0, seed=4)
+    net.make_held_out(0.02, seed=4)
+    for dtype in (_native.PI_F32, _native.PI_BF16):
+        s, opts = make_sampler(net, dtype, K=1024, num_node_sample=40, mini_batch_size=64)
+        phi, theta = random_state(net.N, 1024, seed=2)
+        s.set_state(phi, theta)
+        mb, nbrs, nby, pn, tn = fed_inputs(net, s, opts, 3)
+        s.step_fed(3, np.stack([mb["edge_a"], mb["edge_b"]], 1), mb["edge_y"], mb["scale"],
+                   mb["nodes"], nbrs, nby, pn, tn)
+        idx = mb["nodes"]
+        if dtype == _native.PI_F32:
+            want_phi, _, want_th, _ = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs,
+                                                      nby, pn, tn, 3, np.float32)
+            assert rel_err(s.phi[idx], want_phi[idx]) < RTOL_STEP
+            assert rel_err(s.theta, want_th) < RTOL_STEP
+        else:
+            # BF16 neighbour rows: the step against the f64 oracle on the
+            # BF16-rounded pi is the meaningful comparison
+            f_phi, _, f_th, _ = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby,
+                                                pn, tn, 3, np.float64)
+            assert rel_err(s.phi[idx], f_phi[idx]) < 5e-3
+        s.close()
+
+
+# ---------------------------------------------------------------------------
+# perplexity
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("K", [32, 24])
+def test_perplexity_matches_oracle(small, K):
+    net, _ = small
+    s, opts = make_sampler(net, K=K)
+    phi, theta = random_state(net.N, K, seed=11)
+    s.set_state(phi, theta)
+    pi = s.pi
+    beta = s.beta
+    ppx = np.zeros(len(net.held_out[0]), np.float32)
+    for c in (1, 2, 3):
+        got = s.cal_perplexity_held_out()
+        want = oracle.perplexity(K, pi, net.held_out, beta, s.resolved.epsilon, ppx, c, "f64acc")
+        assert got == pytest.approx(want, rel=RTOL_PPX)
+        assert rel_err(s.ppx_per_heldout_edge, ppx) < 1e-5
+    ref = oracle.perplexity(K, pi, net.held_out, beta, s.resolved.epsilon,
+                            np.zeros_like(ppx), 1, "f32")
+    assert np.isfinite(ref)
+    s.close()
+
+
+# ---------------------------------------------------------------------------
+# trajectories
+# ---------------------------------------------------------------------------
+def run_trajectory(s, iters, interval):
+    out = []
+    for it in range(iters):
+        if it % interval == 0:
+            out.append(s.cal_perplexity_held_out())
+        s.step(1)
+    return np.array(out)
+
+
+def test_trajectory_small_vs_oracle(small):
+    """The small workload (2,000 iterations, perplexity every 100): GPU FP32
+    against the oracle sampler with the same Philox draws."""
+    net, opts = small
+    s = MCMCSamplerStochastic(opts, net).create()
+    phi, theta = random_state(net.N, 32, seed=21)
+    s.set_state(phi, theta)
+    r = s.resolved
+    orc = oracle.OracleSampler(net, 32, mini_batch_size=r.mini_batch_size,
+                               num_node_sample=r.num_node_sample, alpha=r.alpha,
+                               epsilon=r.epsilon, a=r.a, b=r.b, c=r.c, seed=r.random_seed)
+    orc.set_state(phi, theta)
+    got, want = [], []
+    for it in range(2000):
+        if it % 100 == 0:
+            got.append(s.cal_perplexity_held_out())
+            want.append(orc.perplexity())
+        s.step(1)
+        orc.step()
+    got, want = np.array(got), np.array(want)
+    assert np.all(np.abs(got - want) <= 0.01 * np.abs(want)), (got, want)
+    s.close()
+
+
+def test_trajectory_bf16_within_1pct_of_f32(small):
+    net, opts = small
+    traj = {}
+    for dtype in (_native.PI_F32, _native.PI_BF16):
+        o = Options(**{k: getattr(opts, k) for k in ("K", "alpha", "a", "b", "c", "num_node_sample",
+                                                     "held_out_ratio")}, pi_dtype=dtype)
+        s = MCMCSamplerStochastic(o, net).create()
+        s.set_state(*random_state(net.N, 32, seed=21))
+        traj[dtype] = run_trajectory(s, 2000, 100)
+        s.close()
+    f32, bf16 = traj[_native.PI_F32], traj[_native.PI_BF16]
+    assert np.all(np.abs(bf16 - f32) <= 0.01 * np.abs(f32)), (f32, bf16)
+
+
+# ---------------------------------------------------------------------------
+# init, driver loop, errors
+# ---------------------------------------------------------------------------
+def test_init_state(small):
+    net, _ = small
+    s, opts = make_sampler(net)
+    s.init()
+    phi = s.phi
+    assert abs(phi.mean() - 1.0) < 0.02 and abs(phi.var() - 1.0) < 0.05
+    assert np.allclose(s.pi.sum(1), 1.0, atol=1e-5)
+    # theta follows the host gamma stream; the oracle computes the same draws
+    want = np.array([[oracle.lib().oracle_gamma(42, 0, oracle.P_THETA_INIT, 0, 2 * k + c,
+                                                1.0, 1.0) for c in range(2)] for k in range(32)])
+    assert rel_err(s.theta, want) < 1e-12
+    # phi on the device: the same Marsaglia-Tsang stream in device FP64
+    sub = np.array([[oracle.lib().oracle_gamma(42, 0, oracle.P_PHI_INIT, v, k, 1.0, 1.0)
+                     for k in range(32)] for v in range(50)], np.float32)
+    assert rel_err(phi[:50], sub) < 1e-6
+    s.close()
+
+
+def test_run_prints_reference_lines(small, capfd):
+    net, opts = small
+    o = Options(K=32, num_node_sample=32, max_iteration=201, interval=100, held_out_ratio=0.02)
+    s = MCMCSamplerStochastic(o, net).create()
+    s.init()
+    last = s.run()
+    out = capfd.readouterr().out.strip().splitlines()
+    lines = [l for l in out if l.startswith("average_count is:")]
+    assert len(lines) == 3
+    assert lines[0].startswith("average_count is: 1 step count: 1 time: ")
+    assert lines[2].startswith("average_count is: 3 step count: 201 time: ")
+    assert float(lines[2].split()[-1]) == pytest.approx(last, rel=1e-12)
+    assert s.step_count == 201
+    s.close()
+
+
+def test_errors(small):
+    net, _ = small
+    with pytest.raises(_native.AmmsbError) as e:
+        MCMCSamplerStochastic(Options(K=0), net).create()
+    assert e.value.code == -1
+    with pytest.raises(_native.AmmsbError) as e:
+        MCMCSamplerStochastic(Options(K=16, strategy=3), net).create()
+    assert e.value.code == -6
+    s, _ = make_sampler(net)
+    with pytest.raises(_native.AmmsbError) as e:
+        s.step(1)
+    assert e.value.code == -5
+    s.close()
