@@ -1,0 +1,391 @@
+"""Benchmark of the GB300 SG-MCMC sampler: sampled edge evaluations per
+second of the a-MMSB stochastic-gradient iteration.
+
+One "step" is one SG-MCMC iteration on the large synthetic workload
+(N=4,000,000 nodes, ~43M edges, K=1024, num-node-sample 128, minibatch
+4,096, BF16 pi with FP32 phi master): stratified minibatch + neighbour
+sampling, update_phi, pi, update_beta/theta, all resident in HBM.
+
+  python bench.py [--steps K] [--warmup W] [--workload large|mid|small]
+                  [--pi-dtype bf16|f32] [--impl ours|reference]
+
+Prints one JSON line.  `value` is device-timed (CUDA events on the
+sampler's stream around K captured-graph iterations); `e2e` times the
+public run() loop (perplexity every `interval` iterations, host reads)
+with the host clock; `roofline` is the update_phi kernel's algorithmic
+bytes over its per-launch CUDA-event duration; `cpu_baseline` is the
+oracle's restatement of the reference sampler timed on a bounded sample of
+the same workload on this host.  --impl reference times that CPU
+implementation alone (all host threads) and prints the reference line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SG-MCMC edge-evals/s & time-to-perplexity, BF16-pi vs FP32 plain, 1 GB300"
+UNIT = "edge-evals/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def phi_bytes_per_eval(K, pi_bytes, n_out):
+    """Algorithmic bytes of update_phi per sampled edge evaluation: the
+    neighbour pi row (K * s_pi) and id (4), plus the node's own traffic
+    (pi_i read, pi_i write, phi read + write: K * (2 s_pi + 8)) shared by
+    its n_out evaluations."""
+    return K * pi_bytes + 4 + K * (2 * pi_bytes + 8) / n_out
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle's restatement of the reference sampler
+# ---------------------------------------------------------------------------
+def cpu_sample(net, opts, seconds, threads, max_steps=None, per_step_nodes=512,
+               pool_rows=1 << 18, seed=0):
+    """Times the reference's per-node work -- neighbour sampling
+    (mcmc_sampler_stochastic.h:87-108) and update_phi (cc:269-313) -- as
+    restated by the oracle, on minibatches of this workload drawn by the
+    sampling spec.  Gathered pi rows come from a pool of `pool_rows` rows
+    (ids mapped modulo the pool) instead of the full N x K array, keeping
+    host memory bounded; the arithmetic per edge evaluation is unchanged.
+    Returns (edge_evals, seconds, steps, nodes)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+
+    K = opts.K
+    N = net.N
+    og = oracle.OracleGraph(net)
+    rng = np.random.default_rng(seed)
+    P = min(pool_rows, N)
+    pool = rng.gamma(1.0, 1.0, (P, K)).astype(np.float32)
+    pool /= pool.sum(1, keepdims=True)
+    beta = rng.uniform(0.05, 0.95, K).astype(np.float32)
+    m = opts.mini_batch_size or N // 10
+    nns = opts.num_node_sample or N // 50
+    n_out = nns + 1
+    a = opts.a if opts.a else opts.b ** -opts.c
+    alpha = opts.alpha if opts.alpha else 1.0 / K
+    max_edges = max(m, net.max_degree())
+
+    def node_work(node, step):
+        nb, y = oracle.sample_neighbors(og, node, n_out, 42, 0, step)
+        # local pi over the node and its neighbours (pool rows)
+        rows = np.concatenate([[node], nb]) % P
+        local = pool[rows]
+        lnb = np.arange(1, n_out + 1, dtype=np.int32)
+        phi_i = local[0] * np.float32(K)
+        noise = np.zeros(K, np.float32)
+        oracle.update_phi(K, local, phi_i, 0, lnb, y, beta, alpha, opts.epsilon, 0.01, N, nns,
+                          noise)
+        return n_out
+
+    evals = 0
+    nodes_done = 0
+    steps = 0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        step = 1
+        while True:
+            mb = oracle.sample_minibatch(og, opts.strategy, m, net.num_total_edges, 42, 0, step,
+                                         max_edges)
+            nodes = mb["nodes"][:per_step_nodes]
+            evals += sum(ex.map(lambda v: node_work(int(v), step), nodes))
+            nodes_done += len(nodes)
+            steps += 1
+            step += 1
+            el = time.perf_counter() - t0
+            if max_steps is not None:
+                if steps >= max_steps:
+                    break
+            elif el >= seconds:
+                break
+    return evals, time.perf_counter() - t0, steps, nodes_done
+
+
+def reference_arm(args, net, opts):
+    threads = os.cpu_count() or 1
+    # warm-up steps, then K timed steps (each a bounded per-iteration sample)
+    cpu_sample(net, opts, 0, threads, max_steps=args.warmup, per_step_nodes=args.ref_nodes)
+    ev, secs, steps, nodes = cpu_sample(net, opts, 0, threads, max_steps=args.steps,
+                                        per_step_nodes=args.ref_nodes, seed=1)
+    value = ev / secs
+    sample = ("oracle restatement of neighbour sampling + update_phi, FP32, on up to %d "
+              "minibatch nodes per iteration of the %s workload (%d iterations, %d nodes, "
+              "%d edge evaluations); pi rows from a 2^18-row pool" %
+              (args.ref_nodes, args.workload, steps, nodes, ev))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(args, net, opts),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def workload_config(args, net, opts):
+    return {"workload": args.workload, "N": net.N, "E": net.num_total_edges, "K": opts.K,
+            "num_node_sample": opts.num_node_sample, "mini_batch_size": opts.mini_batch_size,
+            "strategy": args.strategy, "pi_dtype": args.pi_dtype,
+            "held_out": int(net.held_out[0].shape[0]),
+            "l2": "inputs larger than L2 (pi %.1f GB)" % (net.N * opts.K * (2 if args.pi_dtype == "bf16" else 4) / 1e9)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def ours_arm(args, net, opts, rank, world, local):
+    import torch
+    from mcmc_for_ammsb_gb300 import MCMCSamplerStochastic, _native
+
+    torch.cuda.set_device(local)
+    opts.device = local
+    opts.chain = rank  # independent replicas (the path does not shard)
+    opts.pi_dtype = _native.PI_BF16 if args.pi_dtype == "bf16" else _native.PI_F32
+    s = MCMCSamplerStochastic(opts, net).create()
+    s.init()
+    stream = torch.cuda.ExternalStream(s.stream())
+    K = s.K
+    n_out = s.num_node_sample + 1
+    pi_bytes = 2 if args.pi_dtype == "bf16" else 4
+
+    s.step(args.warmup)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0, i0 = s.counters()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev_start = torch.cuda.Event(enable_timing=True)
+    ev_stop = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev_start.record(stream)
+    s.step(args.steps)
+    ev_stop.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev_start.elapsed_time(ev_stop)
+    e1, i1 = s.counters()
+    evals = e1 - e0
+    t = torch.tensor([ms / 1000.0, float(evals)], dtype=torch.float64)
+    if world > 1:
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
+        tsum = t.clone()
+        torch.distributed.all_reduce(tsum[1:], op=torch.distributed.ReduceOp.SUM)
+        secs, total_evals = float(tmax[0]), float(tsum[1])
+    else:
+        secs, total_evals = float(t[0]), float(t[1])
+    value = total_evals / secs
+
+    # per-phase CUDA-event durations of the same iteration (not captured),
+    # for the roofline of the dominant kernel
+    phase = {k: [] for k in ("sample_mini_batch", "sample_neighbor_nodes", "update_phi",
+                             "update_pi+beta_grads", "update_theta")}
+    phi_bytes, phi_ms = 0.0, 0.0
+    nl_bytes, nl_ms, nl_n = 0.0, 0.0, 0
+    m_nodes = (s.resolved.mini_batch_size + 1) * n_out
+    for _ in range(args.profile_steps):
+        ea, _ = s.counters()
+        p = s.profile_step()
+        eb, _ = s.counters()
+        for k, v in p.items():
+            phase[k].append(v)
+        by = (eb - ea) * phi_bytes_per_eval(K, pi_bytes, n_out)
+        phi_bytes += by
+        phi_ms += p["update_phi"]
+        if eb - ea == m_nodes:  # a non-link stratum launch (m + 1 nodes)
+            nl_bytes += by
+            nl_ms += p["update_phi"]
+            nl_n += 1
+    peaks, peak_src = load_peaks()
+    achieved = phi_bytes / (phi_ms / 1000.0) / 1e9 if phi_ms > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "update_phi_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tr = json.load(f)
+        if tr.get("workload") == args.workload and tr.get("pi_dtype") == args.pi_dtype:
+            traffic = tr.get("bytes_per_launch")
+
+    # e2e: the public run() loop (perplexity every interval, host reads)
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        interval = opts.interval or 50
+        ea, _ = s.counters()
+        t0 = time.perf_counter()
+        n_ppx = 0
+        done = 0
+        while done < args.steps:
+            if done % interval == 0:
+                s.cal_perplexity_held_out()  # D2H of the perplexity, synchronises
+                n_ppx += 1
+            n = min(interval - done % interval, args.steps - done)
+            s.step(n)
+            done += n
+        s.beta  # the iteration's global parameters read back (D2H, synchronises)
+        t1 = time.perf_counter()
+        eb, _ = s.counters()
+        e2e = {"value": (eb - ea) / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": (8 * n_ppx + 4 * K) / args.steps,
+               "note": "public API loop: step() with held-out perplexity every %d iterations "
+                       "(its D2H read), beta read back at the end, host clock; minibatch and "
+                       "neighbour draws are generated on the device, so an iteration has no "
+                       "host input to copy" % interval}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        ev, secs_cpu, steps_cpu, nodes_cpu = cpu_sample(net, opts, args.cpu_seconds, 1,
+                                                        per_step_nodes=args.ref_nodes)
+        cpu = {"value": ev / secs_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "oracle restatement (FP32, reference operation order) of neighbour "
+                         "sampling + update_phi on %d minibatch nodes (%d iterations, up to %d "
+                         "nodes each) of this workload, %.1f s on 1 host core" %
+                         (nodes_cpu, steps_cpu, args.ref_nodes, secs_cpu)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16-pi/f32" if args.pi_dtype == "bf16" else "f32",
+            "data": "synthetic (planted-community generator, seed 0)",
+            "config": dict(workload_config(args, net, opts),
+                           parallelism="replicas" if world > 1 else "single"),
+            "iterations_per_s": (i1 - i0) / secs if world == 1 else None,
+            "gpu_launches": 5 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved,
+                         "peak": peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]),
+                         "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0),
+                         "traffic": traffic, "kernel": "k_update_phi",
+                         "peak_source": peak_src,
+                         "launches": args.profile_steps,
+                         "nonlink_launches": nl_n,
+                         "nonlink_achieved": (nl_bytes / (nl_ms / 1000.0) / 1e9) if nl_ms else None,
+                         "nonlink_ms": (nl_ms / nl_n) if nl_n else None},
+            "phase_ms_mean": {k: statistics.mean(v) for k, v in phase.items() if v},
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    s.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large", choices=["large", "large_s", "mid", "small"])
+    ap.add_argument("--strategy", default="stratified-random-node",
+                    choices=["stratified-random-node", "stratified-random-node-links",
+                             "stratified-random-node-nonlinks"])
+    ap.add_argument("--pi-dtype", default="bf16", choices=["bf16", "f32"])
+    ap.add_argument("--profile-steps", type=int, default=40)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-nodes", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank, world, local = dist_env()
+    if args.impl == "reference" and rank != 0:
+        return
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    from mcmc_for_ammsb_gb300 import workloads
+    from mcmc_for_ammsb_gb300.options import STRATEGIES
+    net, opts = workloads.build(args.workload, strategy=STRATEGIES[args.strategy])
+    if args.impl == "reference":
+        reference_arm(args, net, opts)
+    else:
+        ours_arm(args, net, opts, rank, world, local)
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -182,6 +182,12 @@ int ammsb_profile_step(ammsb_handle *h, double *ms5);
  * order their own work against it. */
 void *ammsb_stream(ammsb_handle *h);
 
+/* Device-side running totals since the last init/set_state: sampled edge
+ * evaluations (sum over iterations of minibatch nodes x (num_node_sample
+ * + 1), the unit of the edge-evals/s metric) and sampled iterations. */
+int ammsb_get_counters(ammsb_handle *h, uint64_t *edge_evals,
+                       uint64_t *iterations);
+
 /* ------------------------------------------------------------------------ */
 /* Host-side data preparation (no GPU use).                                 */
 /* ------------------------------------------------------------------------ */

@@ -127,6 +127,7 @@ SIGNATURES = [
     ("ammsb_get_options", ctypes.c_int, [_P, ctypes.POINTER(AmmsbOptions)]),
     ("ammsb_profile_step", ctypes.c_int, [_P, _F64P]),
     ("ammsb_stream", _P, [_P]),
+    ("ammsb_get_counters", ctypes.c_int, [_P, _U64P, _U64P]),
     ("ammsb_generate_graph", ctypes.c_int, [ctypes.POINTER(AmmsbGenParams), ctypes.POINTER(_P)]),
     ("ammsb_graph_from_edges", ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _I32P, _I32P,
                                               ctypes.POINTER(_P)]),

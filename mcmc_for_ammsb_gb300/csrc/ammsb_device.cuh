@@ -29,7 +29,10 @@ struct DevState {
   int32_t n_nodes;
   int32_t rounds;
   int32_t err;
-  int32_t pad[7];
+  int32_t pad;
+  unsigned long long evals;  // running sum of n_nodes * n_out (edge evaluations)
+  unsigned long long iters;  // running count of sampled iterations
+  int32_t pad2[2];
 };
 
 // Graph in device memory: symmetric CSR with sorted rows, plus an

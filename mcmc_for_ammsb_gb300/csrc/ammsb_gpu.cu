@@ -10,12 +10,14 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/ammsb_gpu.h"
 #include "ammsb_kernels.cuh"
+#include "ammsb_phi_tma.cuh"
 
 using namespace ammsb;
 
@@ -58,6 +60,7 @@ double host_gamma(const Stream& s, uint32_t tag, uint32_t entity, uint64_t idx,
 
 struct KernelCfg {
   int lpn, vpl, split, npb;  // update_phi
+  int tma;                   // wide rows: bulk-copy pipeline kernel
   int ppx_lpn, ppx_vpl;      // perplexity
   int kq;                    // commit_beta
 };
@@ -129,9 +132,38 @@ cudaError_t launch_phi_t(ammsb_handle* h, const Buffers& b) {
   return cudaGetLastError();
 }
 
+constexpr int kTmaSplit = 4;
+constexpr int kTmaStages = 4;
+
+template <typename PiT, int VPL>
+cudaError_t launch_phi_tma_t(ammsb_handle* h, const Buffers& b, bool configure) {
+  auto kern = k_update_phi_tma<PiT, VPL, kTmaSplit, kTmaStages>;
+  const size_t smem = PhiTmaSmem<PiT, VPL, kTmaSplit, kTmaStages>::bytes(h->m.Kp, h->m.n_out);
+  if (configure) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    h->phi_smem = smem;
+    return cudaSuccess;
+  }
+  kern<<<h->m.max_nodes, kTmaSplit * 32, smem, h->stream>>>(h->m, b);
+  return cudaGetLastError();
+}
+
+template <typename PiT>
+cudaError_t launch_phi_tma(ammsb_handle* h, const Buffers& b, bool configure) {
+  switch (h->cfg.vpl) {
+    case 1: return launch_phi_tma_t<PiT, 1>(h, b, configure);
+    case 2: return launch_phi_tma_t<PiT, 2>(h, b, configure);
+    case 4: return launch_phi_tma_t<PiT, 4>(h, b, configure);
+    case 8: return launch_phi_tma_t<PiT, 8>(h, b, configure);
+    default: return cudaErrorInvalidConfiguration;
+  }
+}
+
 template <typename PiT>
 cudaError_t launch_phi(ammsb_handle* h, const Buffers& b) {
   const KernelCfg& c = h->cfg;
+  if (c.tma) return launch_phi_tma<PiT>(h, b, false);
 #define PHI_CASE(L, V, S) \
   if (c.lpn == L && c.vpl == V && c.split == S) return launch_phi_t<PiT, L, V, S>(h, b);
   PHI_CASE(1, 1, 1) PHI_CASE(2, 1, 1) PHI_CASE(4, 1, 1) PHI_CASE(8, 1, 1) PHI_CASE(16, 1, 1)
@@ -193,7 +225,7 @@ cudaError_t launch_update_phase(ammsb_handle* h, const Buffers& b) {
   e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_commit<__nv_bfloat16>(h, b)
                                           : launch_commit<float>(h, b);
   if (e != cudaSuccess) return e;
-  k_theta<<<(h->m.K + 255) / 256, 256, 0, h->stream>>>(h->m, b);
+  k_theta<<<(h->m.K + 31) / 32, 256, 0, h->stream>>>(h->m, b);
   return cudaGetLastError();
 }
 
@@ -247,6 +279,10 @@ void choose_config(ammsb_handle* h) {
     c.vpl = next_pow2((nvec + 31) / 32);
   }
   c.split = (c.lpn == 32) ? (c.vpl >= 2 ? 4 : 2) : 1;
+  c.tma = (c.lpn == 32) ? 1 : 0;
+  if (const char* env = std::getenv("AMMSB_PHI_KERNEL")) {  // "tma" or "regs"
+    if (std::strcmp(env, "regs") == 0) c.tma = 0;
+  }
   c.npb = std::max(1, 128 / (c.lpn * c.split));
   c.ppx_lpn = c.lpn;
   c.ppx_vpl = c.vpl;
@@ -524,6 +560,14 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
       return bail(AMMSB_E_ARG);
     }
   }
+  if (h->cfg.tma) {
+    cudaError_t e = (o.pi_dtype == AMMSB_PI_BF16) ? launch_phi_tma<__nv_bfloat16>(h, h->b, true)
+                                                   : launch_phi_tma<float>(h, h->b, true);
+    if (e != cudaSuccess) {
+      h->err = std::string("update_phi shared memory configuration: ") + cudaGetErrorString(e);
+      return bail(AMMSB_E_CUDA);
+    }
+  }
   if (reset_counters(h) != AMMSB_OK) return bail(AMMSB_E_CUDA);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
     h->err = std::string("create: ") + cudaGetErrorString(cudaGetLastError());
@@ -535,8 +579,9 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
                  (long long)o.max_iteration);
     std::fprintf(stderr, "num_node_sample %lld\na %g b %g c %g eta (%g,%g)\n",
                  (long long)o.num_node_sample, o.a, o.b, o.c, o.eta0, o.eta1);
-    std::fprintf(stderr, "update_phi lanes/node %d vec/lane %d split %d; pi %s\n", h->cfg.lpn,
-                 h->cfg.vpl, h->cfg.split, o.pi_dtype == AMMSB_PI_BF16 ? "bf16" : "f32");
+    std::fprintf(stderr, "update_phi lanes/node %d vec/lane %d split %d %s; pi %s\n", h->cfg.lpn,
+                 h->cfg.vpl, h->cfg.split, h->cfg.tma ? "bulk-copy pipeline" : "register path",
+                 o.pi_dtype == AMMSB_PI_BF16 ? "bf16" : "f32");
   }
   *out = h;
   return AMMSB_OK;
@@ -746,7 +791,7 @@ int ammsb_run(ammsb_handle* h, double* last) {
       const double secs =
           std::chrono::duration<double>(std::chrono::system_clock::now() - t0).count();
       std::printf("average_count is: %llu step count: %llu time: %.3f perplexity for hold out set: %.12f\n",
-                  (unsigned long long)(h->average_count - 1), (unsigned long long)h->step_count, secs, ppx);
+                  (unsigned long long)h->average_count, (unsigned long long)h->step_count, secs, ppx);
       std::fflush(stdout);
       h->ppx_history.push_back(ppx);
     }
@@ -899,7 +944,7 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
   CK(cudaEventRecord(ev[3], h->stream));
   CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_commit<__nv_bfloat16>(h, h->b) : launch_commit<float>(h, h->b));
   CK(cudaEventRecord(ev[4], h->stream));
-  k_theta<<<(h->m.K + 255) / 256, 256, 0, h->stream>>>(h->m, h->b);
+  k_theta<<<(h->m.K + 31) / 32, 256, 0, h->stream>>>(h->m, h->b);
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[5], h->stream));
   CK(cudaEventSynchronize(ev[5]));
@@ -914,5 +959,16 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
 }
 
 void* ammsb_stream(ammsb_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int ammsb_get_counters(ammsb_handle* h, uint64_t* edge_evals, uint64_t* iterations) {
+  if (!h) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  DevState st;
+  CK(cudaMemcpyAsync(&st, h->b.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (edge_evals) *edge_evals = st.evals;
+  if (iterations) *iterations = st.iters;
+  return AMMSB_OK;
+}
 
 }  // extern "C"

@@ -254,6 +254,10 @@ __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, 
     b.st->n_edges = s_count;
     b.st->n_nodes = err ? 0 : s_count + 1;
     b.st->rounds = rounds;
+    if (!err) {
+      b.st->evals += (unsigned long long)(s_count + 1) * (unsigned long long)m.n_out;
+      b.st->iters += 1ull;
+    }
     if (err) atomicOr(&b.st->err, err);
   }
 }
@@ -616,17 +620,47 @@ __global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int nco
 //   G_k1 = beta R1 (1/theta_k1 - 1/ts) + (1-beta) R0 (0 - 1/ts)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_theta(Model m, Buffers b) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= m.K) return;
+  // 32 consecutive k per CTA; warp w sums block partials w, w+8, ... in FP64,
+  // then warp 0 adds the eight warp sums in fixed order (deterministic).
+  __shared__ double s_r0[8][32], s_r1[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  const int Kp = m.Kp;
+  double r0 = 0.0, r1 = 0.0;
+  if (k < m.K) {
+    int bb = warp;
+    for (; bb + 24 < m.nbb; bb += 32) {
+      const float* p0 = b.beta_part + (int64_t)bb * 2 * Kp + k;
+      const float a0 = p0[0], a1 = p0[8 * 2 * Kp], a2 = p0[16 * 2 * Kp], a3 = p0[24 * 2 * Kp];
+      const float c0 = p0[Kp], c1 = p0[8 * 2 * Kp + Kp], c2 = p0[16 * 2 * Kp + Kp],
+                  c3 = p0[24 * 2 * Kp + Kp];
+      r0 += (double)a0;
+      r0 += (double)a1;
+      r0 += (double)a2;
+      r0 += (double)a3;
+      r1 += (double)c0;
+      r1 += (double)c1;
+      r1 += (double)c2;
+      r1 += (double)c3;
+    }
+    for (; bb < m.nbb; bb += 8) {
+      r0 += (double)b.beta_part[(int64_t)bb * 2 * Kp + k];
+      r1 += (double)b.beta_part[(int64_t)bb * 2 * Kp + Kp + k];
+    }
+  }
+  s_r0[warp][lane] = r0;
+  s_r1[warp][lane] = r1;
+  __syncthreads();
+  if (warp != 0 || k >= m.K) return;
+  double R0 = 0.0, R1 = 0.0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    R0 += s_r0[w][lane];
+    R1 += s_r1[w][lane];
+  }
   const uint32_t step = b.st->step;
   const double eps_t = (double)b.st->eps;
   const double scale = (double)b.st->scale;
-  const int Kp = m.Kp;
-  double R0 = 0.0, R1 = 0.0;
-  for (int bb = 0; bb < m.nbb; ++bb) {
-    R0 += (double)b.beta_part[(int64_t)bb * 2 * Kp + k];
-    R1 += (double)b.beta_part[(int64_t)bb * 2 * Kp + Kp + k];
-  }
   const double th0 = b.theta[2 * k], th1 = b.theta[2 * k + 1];
   const double ts_inv = 1.0 / (th0 + th1);
   const double bt = (double)b.beta[k];

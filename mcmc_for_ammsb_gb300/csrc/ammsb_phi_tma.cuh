@@ -1,0 +1,331 @@
+// ammsb_phi_tma.cuh -- update_phi for wide pi rows (>= 512 bytes), with the
+// neighbour rows staged in shared memory by the Blackwell bulk-copy engine.
+//
+// One CTA per minibatch node, SPLIT warps.  Warp g handles neighbours
+// g, g+SPLIT, ...: its lane 0 keeps STAGES row copies in flight
+// (cp.async.bulk global -> shared, completion counted on one mbarrier per
+// stage); every lane waits on the stage's barrier, reads its 16-byte
+// vectors of the row from shared memory and does the two FMA passes of the
+// factored gradient (see k_update_phi in ammsb_kernels.cuh for the algebra).
+// All waits are bounded: a wait that runs out sets kErrPipeline, drains the
+// copies this warp still has in flight (also bounded) and the CTA skips its
+// phi write, so a stuck copy cannot hang the GPU.
+#pragma once
+#include "ammsb_kernels.cuh"
+
+namespace ammsb {
+
+enum : int32_t { kErrPipeline = 16 };
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: gives up after 200 ms (global timer) or 2^24 polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 0; it < (1u << 16); ++it) {
+    for (int r = 0; r < 256; ++r)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > 200000000ull) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+template <typename PiT, int VPL, int SPLIT, int STAGES>
+struct PhiTmaSmem {
+  static size_t bytes(int Kp, int n_out) {
+    size_t ring = (size_t)SPLIT * STAGES * Kp * sizeof(PiT);
+    size_t bars = (size_t)SPLIT * STAGES * sizeof(uint64_t);
+    size_t w = (size_t)Kp * sizeof(float);
+    size_t A = (size_t)SPLIT * Kp * sizeof(float);
+    size_t misc = (size_t)(4 * SPLIT + 8) * sizeof(float) + (size_t)n_out * sizeof(uint32_t);
+    return ring + bars + w + A + misc + 128;
+  }
+};
+
+template <typename PiT, int VPL, int SPLIT, int STAGES>
+__global__ void __launch_bounds__(SPLIT * 32) k_update_phi_tma(Model m, Buffers b) {
+  using TR = PiTraits<PiT>;
+  constexpr int EV = TR::kPerVec;
+  constexpr int EPL = VPL * EV;
+  constexpr int NT = SPLIT * 32;
+  extern __shared__ __align__(128) unsigned char s_raw[];
+  const int Kp = m.Kp, K = m.K, n_out = m.n_out;
+  PiT* ring = reinterpret_cast<PiT*>(s_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ring + (size_t)SPLIT * STAGES * Kp);
+  float* s_w = reinterpret_cast<float*>(bars + SPLIT * STAGES);
+  float* s_A = s_w + Kp;
+  float* s_red = s_A + (size_t)SPLIT * Kp;  // 4*SPLIT + 8 floats
+  uint32_t* s_nb = reinterpret_cast<uint32_t*>(s_red + 4 * SPLIT + 8);
+  __shared__ int s_broken;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_nodes = b.st->n_nodes;
+  const uint32_t step = b.st->step;
+  const float eps_t = b.st->eps;
+  const PiT* __restrict__ pi = reinterpret_cast<const PiT*>(b.pi);
+  const uint32_t row_bytes = (uint32_t)(Kp * sizeof(PiT));
+  const int nvec = Kp / EV;
+  const Stream rs{m.seed, m.chain};
+
+  uint64_t* my_bars = bars + warp * STAGES;
+  PiT* my_ring = ring + (size_t)warp * STAGES * Kp;
+  if (lane == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(my_bars + s, 1);
+    fence_mbar_init();
+  }
+  if (tid == 0) s_broken = 0;
+  __syncthreads();
+  uint32_t seq = 0;    // rows consumed by this warp so far (barrier phase bookkeeping)
+  bool dead = false;   // a bounded wait ran out: this warp issues and waits no more
+
+  for (int slot = blockIdx.x; slot < n_nodes; slot += gridDim.x) {
+    const int32_t i = b.nodes[slot];
+    const float* phi_i = b.phi + (int64_t)i * Kp;
+    // ---- node prologue: S = sum phi, s_i = sum pi, w = pi * (beta - eps)
+    float S = 0.f;
+    for (int k = tid; k < Kp; k += NT) S += phi_i[k];
+    for (int q = tid; q < n_out; q += NT) s_nb[q] = b.nbr[(int64_t)slot * n_out + q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+    if (lane == 0) s_red[warp] = S;
+    __syncthreads();
+    S = 0.f;
+#pragma unroll
+    for (int w = 0; w < SPLIT; ++w) S += s_red[w];
+    float si = 0.f;
+    for (int k = tid; k < Kp; k += NT) {
+      const float p = __fdiv_rn(phi_i[k], S);
+      si += p;
+      s_w[k] = (k < K) ? p * (b.beta[k] - m.epsilon) : 0.f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) si += __shfl_xor_sync(0xffffffffu, si, o);
+    if (lane == 0) s_red[SPLIT + warp] = si;
+    __syncthreads();
+    si = 0.f;
+#pragma unroll
+    for (int w = 0; w < SPLIT; ++w) si += s_red[SPLIT + w];
+    const float one_m_si = 1.0f - si;
+
+    // ---- rows of this warp: q = warp + SPLIT * t
+    const int T = (!dead && n_out > warp) ? (n_out - warp + SPLIT - 1) / SPLIT : 0;
+    float w[EPL], A[EPL];
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) {
+      const int vi = lane + 32 * v;
+#pragma unroll
+      for (int e = 0; e < EV; ++e) {
+        w[v * EV + e] = (vi < nvec) ? s_w[vi * EV + e] : 0.f;
+        A[v * EV + e] = 0.f;
+      }
+    }
+    if (lane == 0) {
+      const int pre = T < STAGES ? T : STAGES;
+      for (int t = 0; t < pre; ++t) {
+        const uint32_t sq = seq + t;
+        const int stg = sq % STAGES;
+        const uint32_t j = s_nb[warp + SPLIT * t] & 0x7fffffffu;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(my_bars + stg, row_bytes);
+        bulk_copy_g2s(my_ring + (size_t)stg * Kp, pi + (int64_t)j * Kp, row_bytes, my_bars + stg);
+      }
+    }
+    float Bsum = 0.f;
+    bool broken = false;
+    int t = 0;
+    for (; t < T; ++t) {
+      const uint32_t sq = seq + t;
+      const int stg = sq % STAGES;
+      if (!mbar_wait_bounded(my_bars + stg, (sq / STAGES) & 1u)) {
+        broken = true;
+        break;
+      }
+      const PiT* row = my_ring + (size_t)stg * Kp;
+      float D = 0.f;
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = lane + 32 * v;
+        if (vi < nvec) {
+          float x[EV];
+          TR::unpack(*reinterpret_cast<const uint4*>(row + vi * EV), x);
+#pragma unroll
+          for (int e = 0; e < EV; ++e) D = fmaf(w[v * EV + e], x[e], D);
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) D += __shfl_xor_sync(0xffffffffu, D, o);
+      const uint32_t word = s_nb[warp + SPLIT * t];
+      const bool y = (word >> 31) != 0;
+      const float sgn = y ? 1.f : -1.f;
+      const float ej = y ? m.epsilon : 1.0f - m.epsilon;
+      const float P = fmaf(sgn, D, ej * si);
+      const float invP = __frcp_rn(P);
+      const float cj = sgn * invP;
+      Bsum += (ej * one_m_si - sgn * D) * invP;
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = lane + 32 * v;
+        if (vi < nvec) {
+          float x[EV];
+          TR::unpack(*reinterpret_cast<const uint4*>(row + vi * EV), x);
+#pragma unroll
+          for (int e = 0; e < EV; ++e) A[v * EV + e] = fmaf(cj, x[e], A[v * EV + e]);
+        }
+      }
+      __syncwarp();
+      if (lane == 0 && t + STAGES < T) {  // refill this stage with row t + STAGES
+        const uint32_t j = s_nb[warp + SPLIT * (t + STAGES)] & 0x7fffffffu;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(my_bars + stg, row_bytes);
+        bulk_copy_g2s(my_ring + (size_t)stg * Kp, pi + (int64_t)j * Kp, row_bytes, my_bars + stg);
+      }
+    }
+    if (broken) {
+      // drain the copies still in flight for rows t .. min(T, t+STAGES)-1
+      dead = true;
+      const int last = (T < t + STAGES) ? T : t + STAGES;
+      for (int u = t; u < last; ++u) {
+        const uint32_t sq = seq + u;
+        mbar_wait_bounded(my_bars + sq % STAGES, (sq / STAGES) & 1u);
+      }
+      if (lane == 0) {
+        atomicOr(&b.st->err, kErrPipeline);
+        s_broken = 1;
+      }
+    }
+    seq += T;
+    // ---- publish A, B; epilogue over all NT threads
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) {
+      const int vi = lane + 32 * v;
+      if (vi < nvec) {
+#pragma unroll
+        for (int e = 0; e < EV; ++e) s_A[(size_t)warp * Kp + vi * EV + e] = A[v * EV + e];
+      }
+    }
+    if (lane == 0) s_red[2 * SPLIT + warp] = Bsum;
+    __syncthreads();
+    float Bt = 0.f;
+#pragma unroll
+    for (int w2 = 0; w2 < SPLIT; ++w2) Bt += s_red[2 * SPLIT + w2];
+    const float invS = 1.0f / S;
+    const float half_eps = eps_t / 2.0f;
+    const bool write = (s_broken == 0);
+    float* phi_w = b.phi + (int64_t)i * Kp;
+    // thread handles 4 consecutive elements per group: one Philox block
+    // gives their four normals
+    constexpr int NG = (VPL * EV * 32 + 4 * NT - 1) / (4 * NT);
+    float pn[NG][4];
+    float Snew = 0.f;
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int k0 = 4 * (tid + NT * g);
+      float nz[4] = {0.f, 0.f, 0.f, 0.f};
+      if (k0 < K) {
+        if (b.fed_phi_noise) {
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            nz[e] = (k0 + e < K) ? b.fed_phi_noise[(int64_t)slot * K + k0 + e] : 0.f;
+        } else {
+          const U32x4 o = rs.block(kTagPhiNoise, (uint32_t)i, step, (uint64_t)k0 >> 2);
+          float s0, c0, s1, c1;
+          const float r0 = sqrtf(-2.0f * logf(u24_open(o.x)));
+          const float r1 = sqrtf(-2.0f * logf(u24_open(o.z)));
+          sincospif(2.0f * u24(o.y), &s0, &c0);
+          sincospif(2.0f * u24(o.w), &s1, &c1);
+          nz[0] = r0 * c0;
+          nz[1] = r0 * s0;
+          nz[2] = r1 * c1;
+          nz[3] = r1 * s1;
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int k = k0 + e;
+        float val = 0.f;
+        if (k < K) {
+          float Ak = 0.f;
+#pragma unroll
+          for (int s = 0; s < SPLIT; ++s) Ak += s_A[(size_t)s * Kp + k];
+          const float bk = b.beta[k] - m.epsilon;
+          const float grad = (bk * Ak + Bt) * invS;
+          const float ph = phi_i[k];
+          val = fabsf((ph + half_eps * (m.alpha - ph + m.Nn * grad)) + sqrtf(eps_t * ph) * nz[e]);
+          if (val < 1.0e-24f) val = 1.0e-24f;
+          if (write) phi_w[k] = val;
+        }
+        pn[g][e] = val;
+        Snew += val;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) Snew += __shfl_xor_sync(0xffffffffu, Snew, o);
+    if (lane == 0) s_red[3 * SPLIT + warp] = Snew;
+    __syncthreads();
+    Snew = 0.f;
+#pragma unroll
+    for (int w2 = 0; w2 < SPLIT; ++w2) Snew += s_red[3 * SPLIT + w2];
+    float* st = b.stage + (int64_t)slot * Kp;
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const int k0 = 4 * (tid + NT * g);
+      if (k0 < Kp) {
+        float4 o;
+        o.x = (k0 + 0 < K) ? __fdiv_rn(pn[g][0], Snew) : 0.f;
+        o.y = (k0 + 1 < K) ? __fdiv_rn(pn[g][1], Snew) : 0.f;
+        o.z = (k0 + 2 < K) ? __fdiv_rn(pn[g][2], Snew) : 0.f;
+        o.w = (k0 + 3 < K) ? __fdiv_rn(pn[g][3], Snew) : 0.f;
+        *reinterpret_cast<float4*>(st + k0) = o;
+      }
+    }
+    __syncthreads();  // smem reuse by the next node
+  }
+}
+
+}  // namespace ammsb

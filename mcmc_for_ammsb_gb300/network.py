@@ -20,24 +20,34 @@ def _as_np(ptr, n, dtype):
 
 
 class Network:
-    def __init__(self, row_ptr, col, held_out=None, test=None):
+    def __init__(self, row_ptr, col, held_out=None, test=None, _buf=None):
         self.row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
         self.col = np.ascontiguousarray(col, dtype=np.int32)
         self.N = int(self.row_ptr.shape[0] - 1)
         z = (np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint8))
         self.held_out = held_out if held_out is not None else z
         self.test = test if test is not None else z
+        self._buf = _buf  # native ammsb_graph_buf owning the same CSR, if any
+
+    def __del__(self):
+        buf, self._buf = getattr(self, "_buf", None), None
+        if buf is not None:
+            try:
+                _native.lib().ammsb_graph_free(buf)
+            except Exception:
+                pass
 
     # -- construction -----------------------------------------------------
     @staticmethod
     def _from_buf(buf):
+        """Network over a native graph buffer (takes ownership of it)."""
         L = _native.lib()
         view = _native.AmmsbGraph()
         L.ammsb_graph_view(buf, ctypes.byref(view))
         n = view.n
         row_ptr = _as_np(view.row_ptr, n + 1, np.int64)
         col = _as_np(view.col, int(row_ptr[-1]), np.int32)
-        return Network(row_ptr, col)
+        return Network(row_ptr, col, _buf=buf)
 
     @staticmethod
     def synthetic(n, k_true, size_min=10, size_max=500, zipf_s=1.5, p1=0.7, p2=0.25,
@@ -48,10 +58,7 @@ class Network:
                                    intra_degree, background_frac, seed)
         buf = ctypes.c_void_p()
         _native.check(L.ammsb_generate_graph(ctypes.byref(p), ctypes.byref(buf)))
-        try:
-            return Network._from_buf(buf)
-        finally:
-            L.ammsb_graph_free(buf)
+        return Network._from_buf(buf)
 
     @staticmethod
     def from_edges(n, a, b):
@@ -62,10 +69,7 @@ class Network:
         _native.check(L.ammsb_graph_from_edges(
             n, a.shape[0], a.ctypes.data_as(_native._I32P), b.ctypes.data_as(_native._I32P),
             ctypes.byref(buf)))
-        try:
-            return Network._from_buf(buf)
-        finally:
-            L.ammsb_graph_free(buf)
+        return Network._from_buf(buf)
 
     @staticmethod
     def from_relativity(path, contiguous=False):
@@ -73,14 +77,14 @@ class Network:
         buf = ctypes.c_void_p()
         _native.check(L.ammsb_read_relativity(path.encode(), int(bool(contiguous)),
                                               ctypes.byref(buf)))
-        try:
-            return Network._from_buf(buf)
-        finally:
-            L.ammsb_graph_free(buf)
+        return Network._from_buf(buf)
 
     def _with_buf(self, fn):
-        """Run fn(graph_buf) on a native copy of this graph."""
+        """Run fn(graph_buf) on the native graph (built from the CSR if this
+        Network was not made by the native library)."""
         L = _native.lib()
+        if self._buf is not None:
+            return fn(self._buf)
         und = self.undirected_edges()
         buf = ctypes.c_void_p()
         a = np.ascontiguousarray(und[:, 0])

@@ -188,6 +188,12 @@ class MCMCSamplerStochastic:
                     edge_y=ey[:e], nodes=nodes[:n], nbrs=nbrs[:n * n_out].reshape(n, n_out),
                     nbr_y=nby[:n * n_out].reshape(n, n_out))
 
+    def counters(self):
+        """(edge evaluations, iterations) sampled on the device so far."""
+        e, i = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(_native.lib().ammsb_get_counters(self._h, ctypes.byref(e), ctypes.byref(i)))
+        return e.value, i.value
+
     def stream(self):
         return _native.lib().ammsb_stream(self._h)
 

@@ -40,6 +40,11 @@ WORKLOADS = {
                  seed=0),
         opts=dict(K=1024, num_node_sample=128, mini_batch_size=4096, held_out_ratio=0.002,
                   a=0.01, b=1024.0, c=0.55, interval=100)),
+    # the large workload's kernel shapes on a 10x smaller graph (profiling)
+    "large_s": dict(
+        gen=dict(n=400000, k_true=20000, size_min=10, size_max=20000, intra_degree=16.0, seed=0),
+        opts=dict(K=1024, num_node_sample=128, mini_batch_size=4096, held_out_ratio=0.002,
+                  a=0.01, b=1024.0, c=0.55, interval=100)),
 }
 
 
