@@ -17,22 +17,27 @@ enum : int32_t {
   kErrInitCap = 8        // gamma rejection loop hit its cap
 };
 
-// Per-iteration scalars, resident in device memory so that a captured CUDA
-// graph can replay the iteration without host involvement.
+// Per-iteration scalars of one minibatch buffer set, resident in device
+// memory so that a captured CUDA graph can replay the iteration without host
+// involvement.  The sampler keeps two buffer sets (ping-pong): the draws of
+// iteration t+1 are made while iteration t updates the state.
 struct DevState {
-  uint32_t step;       // step_count of the running iteration
-  uint32_t next_step;  // step_count of the next one
-  float eps;           // eps_t of the running iteration
-  float scale;         // minibatch scale (network.cc:341, 386-390)
-  int32_t flag;        // 0 non-link stratum, 1 link stratum
+  uint32_t step;   // step_count of the iteration these draws belong to
+  float eps;       // eps_t of that iteration
+  float scale;     // minibatch scale (network.cc:341, 386-390)
+  int32_t flag;    // 0 non-link stratum, 1 link stratum
   int32_t n_edges;
   int32_t n_nodes;
   int32_t rounds;
-  int32_t err;
   int32_t pad;
+};
+
+// Sampler-wide counters shared by both buffer sets.
+struct DevCounters {
+  uint32_t next_step;        // step_count the next sampling pass draws for
+  int32_t err;               // error bits
   unsigned long long evals;  // running sum of n_nodes * n_out (edge evaluations)
-  unsigned long long iters;  // running count of sampled iterations
-  int32_t pad2[2];
+  unsigned long long iters;  // running count of updated iterations
 };
 
 // Graph in device memory: symmetric CSR with sorted rows, plus an

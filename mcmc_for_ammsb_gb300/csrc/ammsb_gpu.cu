@@ -68,10 +68,17 @@ struct KernelCfg {
 struct ammsb_handle {
   ammsb_options opt{};
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // the handle's stream: updates, perplexity, copies
+  cudaStream_t side = nullptr;    // draws of the next iteration, overlapped with the update
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   Model m{};
   DevGraph g{};
-  Buffers b{};
+  Buffers b{};        // shared state pointers (bufs[p] add the minibatch buffers)
+  Buffers bufs[2]{};  // ping-pong minibatch buffer sets
+  DevCounters* gc = nullptr;
+  int parity = 0;           // buffer set of the next iteration
+  bool prefetched = false;  // bufs[parity] already holds the next iteration's draws
+  int last = -1;            // buffer set of the last applied iteration
   KernelCfg cfg{};
   int64_t E = 0, H = 0, T = 0;
   int pi_bytes = 4;
@@ -95,7 +102,7 @@ struct ammsb_handle {
   uint64_t average_count = 1;  // learner.cc:30
   std::vector<double> ppx_history;
   bool state_ready = false;
-  cudaGraphExec_t graph_exec = nullptr;
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
   std::string err;
 };
 
@@ -229,29 +236,49 @@ cudaError_t launch_update_phase(ammsb_handle* h, const Buffers& b) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_sampling_phase(ammsb_handle* h) {
-  k_sample_minibatch<<<1, 1024, 0, h->stream>>>(h->m, h->g, h->b);
+// Draws of one iteration (minibatch + neighbour sets) into buffer set b.
+cudaError_t launch_sampling_phase(ammsb_handle* h, const Buffers& b, cudaStream_t s) {
+  k_sample_minibatch<<<1, 1024, 0, s>>>(h->m, h->g, b);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, h->stream>>>(h->m, h->g, h->b);
+  k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, s>>>(h->m, h->g, b);
   return cudaGetLastError();
 }
 
-cudaError_t launch_iteration(ammsb_handle* h) {
-  cudaError_t e = launch_sampling_phase(h);
+// One pipelined iteration on buffer set p: the update of p on the handle's
+// stream, concurrently with the draws of the next iteration into 1 - p on
+// the side stream (fork/join by events; inside a capture these become graph
+// edges).
+cudaError_t launch_pipelined(ammsb_handle* h, int p) {
+  cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
   if (e != cudaSuccess) return e;
-  return launch_update_phase(h, h->b);
+  if ((e = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess) return e;
+  if ((e = launch_update_phase(h, h->bufs[p])) != cudaSuccess) return e;
+  if ((e = launch_sampling_phase(h, h->bufs[1 - p], h->side)) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess) return e;
+  return cudaStreamWaitEvent(h->stream, h->ev_join, 0);
 }
 
 int check_device_err(ammsb_handle* h) {
-  DevState st;
-  CK(cudaMemcpyAsync(&st, h->b.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  DevCounters gc;
+  CK(cudaMemcpyAsync(&gc, h->gc, sizeof(gc), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  if (st.err) {
-    h->err = "device sampling error bits " + std::to_string(st.err);
-    if (st.err & kErrCapacity) return AMMSB_E_CAPACITY;
+  if (gc.err) {
+    h->err = "device error bits " + std::to_string(gc.err) +
+             " (1 minibatch cap, 2 neighbour cap, 4 capacity, 8 init cap, 16 copy pipeline)";
+    if (gc.err & kErrCapacity) return AMMSB_E_CAPACITY;
     return AMMSB_E_SAMPLING;
   }
+  return AMMSB_OK;
+}
+
+// Drops draws made ahead of time (their step no longer follows) and points
+// the device's next draw at the host's step_count.
+int invalidate_prefetch(ammsb_handle* h) {
+  if (!h->prefetched) return AMMSB_OK;
+  h->prefetched = false;
+  uint32_t s = (uint32_t)h->step_count;
+  CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
   return AMMSB_OK;
 }
 
@@ -259,10 +286,13 @@ int reset_counters(ammsb_handle* h) {
   h->step_count = 1;
   h->average_count = 1;
   h->ppx_history.clear();
-  DevState st{};
-  st.next_step = 1;
-  st.step = 1;
-  CK(cudaMemcpyAsync(h->b.st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  h->parity = 0;
+  h->prefetched = false;
+  h->last = -1;
+  DevCounters gc{};
+  gc.next_step = 1;
+  CK(cudaMemcpyAsync(h->gc, &gc, sizeof(gc), cudaMemcpyHostToDevice, h->stream));
+  for (int p = 0; p < 2; ++p) CK(cudaMemsetAsync(h->bufs[p].st, 0, sizeof(DevState), h->stream));
   CK(cudaMemsetAsync(h->d_ppx, 0, sizeof(float) * std::max<int64_t>(h->H, 1), h->stream));
   return AMMSB_OK;
 }
@@ -329,9 +359,14 @@ const char* ammsb_last_error(const ammsb_handle* h) { return h ? h->err.c_str() 
 void ammsb_destroy(ammsb_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
-  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  for (auto& g : h->graph_exec)
+    if (g) cudaGraphExecDestroy(g);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->side) cudaStreamSynchronize(h->side);
   for (void* p : h->allocs) cudaFree(p);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -411,8 +446,11 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
     h->err = "cudaSetDevice failed (no CUDA device?)";
     return bail(AMMSB_E_CUDA);
   }
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    h->err = "cudaStreamCreate failed";
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    h->err = "cudaStreamCreate / cudaEventCreate failed";
     return bail(AMMSB_E_CUDA);
   }
   const int K = (int)o.K;
@@ -532,23 +570,43 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   TRY(dev_alloc(h, &b.stage, (size_t)m.max_nodes * Kp));
   TRY(dev_alloc(h, &b.beta, (size_t)Kp));
   TRY(dev_alloc(h, &b.theta, 2 * (size_t)K));
-  TRY(dev_alloc(h, &b.nodes, (size_t)m.max_nodes));
-  TRY(dev_alloc(h, &b.ea, (size_t)m.max_edges));
-  TRY(dev_alloc(h, &b.eb, (size_t)m.max_edges));
-  TRY(dev_alloc(h, &b.ey, (size_t)m.max_edges));
-  TRY(dev_alloc(h, &b.nbr, (size_t)m.max_nodes * m.n_out));
+  for (int p = 0; p < 2; ++p) {  // ping-pong minibatch buffer sets
+    Buffers& bp = h->bufs[p];
+    TRY(dev_alloc(h, &bp.nodes, (size_t)m.max_nodes));
+    TRY(dev_alloc(h, &bp.ea, (size_t)m.max_edges));
+    TRY(dev_alloc(h, &bp.eb, (size_t)m.max_edges));
+    TRY(dev_alloc(h, &bp.ey, (size_t)m.max_edges));
+    TRY(dev_alloc(h, &bp.nbr, (size_t)m.max_nodes * m.n_out));
+    TRY(dev_alloc(h, &bp.st, 1));
+  }
   TRY(dev_alloc(h, &b.cand, (size_t)o.mini_batch_size));
   const int hcap = next_pow2(std::max<int64_t>(64, 2 * o.mini_batch_size));
   TRY(dev_alloc(h, &b.htab_key, (size_t)hcap));
   TRY(dev_alloc(h, &b.htab_idx, (size_t)hcap));
   b.hmask = (uint32_t)(hcap - 1);
   TRY(dev_alloc(h, &b.beta_part, (size_t)m.nbb * 2 * Kp));
-  TRY(dev_alloc(h, &b.st, 1));
+  TRY(dev_alloc(h, &h->gc, 1));
+  b.gc = h->gc;
   TRY(dev_alloc(h, &h->d_err_init, 1));
   TRY(dev_alloc(h, &h->d_fed_phi_noise, (size_t)m.max_nodes * K));
   TRY(dev_alloc(h, &h->d_fed_theta_noise, 2 * (size_t)K));
   b.fed_phi_noise = nullptr;
   b.fed_theta_noise = nullptr;
+  for (int p = 0; p < 2; ++p) {  // shared state + this set's minibatch arrays
+    Buffers own = h->bufs[p];
+    h->bufs[p] = b;
+    h->bufs[p].nodes = own.nodes;
+    h->bufs[p].ea = own.ea;
+    h->bufs[p].eb = own.eb;
+    h->bufs[p].ey = own.ey;
+    h->bufs[p].nbr = own.nbr;
+    h->bufs[p].st = own.st;
+  }
+  b.nodes = nullptr;
+  b.ea = b.eb = nullptr;
+  b.ey = nullptr;
+  b.nbr = nullptr;
+  b.st = nullptr;
 #undef TRY
   h->ncommit = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 3) / 4, 152 * 8));
   h->nbr_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 7) / 8, 152 * 8));
@@ -653,8 +711,9 @@ int ammsb_set_step(ammsb_handle* h, uint64_t step_count) {
   if (!h || step_count < 1 || step_count > 0xffffffffull) return AMMSB_E_ARG;
   CK(cudaSetDevice(h->device));
   h->step_count = step_count;
+  h->prefetched = false;
   uint32_t s = (uint32_t)step_count;
-  CK(cudaMemcpyAsync(&h->b.st->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return AMMSB_OK;
 }
@@ -666,23 +725,32 @@ int ammsb_step(ammsb_handle* h, int64_t n_iters) {
     return AMMSB_E_STATE;
   }
   CK(cudaSetDevice(h->device));
-  if (h->opt.use_graph && !h->graph_exec && n_iters > 0) {
-    cudaGraph_t graph;
-    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = launch_iteration(h);
-    cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
-    if (e != cudaSuccess || e2 != cudaSuccess) {
-      h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
-      return AMMSB_E_CUDA;
-    }
-    CK(cudaGraphInstantiate(&h->graph_exec, graph, 0));
-    cudaGraphDestroy(graph);
+  if (n_iters == 0) return AMMSB_OK;
+  if (!h->prefetched) {  // draws of the first iteration of this call
+    CK(launch_sampling_phase(h, h->bufs[h->parity], h->stream));
+    h->prefetched = true;
   }
   for (int64_t it = 0; it < n_iters; ++it) {
-    if (h->graph_exec)
-      CK(cudaGraphLaunch(h->graph_exec, h->stream));
-    else
-      CK(launch_iteration(h));
+    const int p = h->parity;
+    if (h->opt.use_graph) {
+      if (!h->graph_exec[p]) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = launch_pipelined(h, p);
+        cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+          h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+          return AMMSB_E_CUDA;
+        }
+        CK(cudaGraphInstantiate(&h->graph_exec[p], graph, 0));
+        cudaGraphDestroy(graph);
+      }
+      CK(cudaGraphLaunch(h->graph_exec[p], h->stream));
+    } else {
+      CK(launch_pipelined(h, p));
+    }
+    h->last = p;
+    h->parity = 1 - p;
   }
   h->step_count += (uint64_t)n_iters;
   return AMMSB_OK;
@@ -723,28 +791,31 @@ int ammsb_step_fed(ammsb_handle* h, uint32_t step, int32_t n_edges, const int32_
     packed[q] = (uint32_t)nbrs[q] | ((nbr_y[q] ? 1u : 0u) << 31);
   }
   CK(cudaSetDevice(h->device));
-  CK(cudaMemcpyAsync(h->b.nodes, nodes, sizeof(int32_t) * n_nodes, cudaMemcpyHostToDevice, h->stream));
+  int rc0 = invalidate_prefetch(h);
+  if (rc0) return rc0;
+  const Buffers& bp = h->bufs[h->parity];
+  CK(cudaMemcpyAsync(bp.nodes, nodes, sizeof(int32_t) * n_nodes, cudaMemcpyHostToDevice, h->stream));
   if (n_edges > 0) {
-    CK(cudaMemcpyAsync(h->b.ea, edge_slot_a, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->b.eb, edge_slot_b, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->b.ey, edge_y, n_edges, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(bp.ea, edge_slot_a, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(bp.eb, edge_slot_b, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(bp.ey, edge_y, n_edges, cudaMemcpyHostToDevice, h->stream));
   }
-  CK(cudaMemcpyAsync(h->b.nbr, packed.data(), sizeof(uint32_t) * packed.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(bp.nbr, packed.data(), sizeof(uint32_t) * packed.size(), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->d_fed_phi_noise, phi_noise, sizeof(float) * (size_t)n_nodes * K, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->d_fed_theta_noise, theta_noise, sizeof(float) * 2 * K, cudaMemcpyHostToDevice, h->stream));
   DevState st{};
   st.step = step;
-  st.next_step = (uint32_t)h->step_count;
   st.eps = (float)(h->m.a * std::pow(1.0 + (double)step / h->m.b, -h->m.c));
   st.scale = scale;
   st.flag = -1;
   st.n_edges = n_edges;
   st.n_nodes = n_nodes;
-  CK(cudaMemcpyAsync(h->b.st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
-  Buffers fb = h->b;
+  CK(cudaMemcpyAsync(bp.st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  Buffers fb = bp;
   fb.fed_phi_noise = h->d_fed_phi_noise;
   fb.fed_theta_noise = h->d_fed_theta_noise;
   CK(launch_update_phase(h, fb));
+  h->last = h->parity;
   return check_device_err(h);
 }
 
@@ -876,23 +947,30 @@ int ammsb_get_last_minibatch(ammsb_handle* h, int32_t* flag, int32_t* n_edges, i
                              int32_t* nbrs, uint8_t* nbr_y) {
   if (!h) return AMMSB_E_ARG;
   CK(cudaSetDevice(h->device));
+  if (h->last < 0) {
+    h->err = "no iteration has run yet";
+    return AMMSB_E_STATE;
+  }
+  const Buffers& bl = h->bufs[h->last];
   DevState st;
-  CK(cudaMemcpyAsync(&st, h->b.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  DevCounters gc;
+  CK(cudaMemcpyAsync(&st, bl.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(&gc, h->gc, sizeof(gc), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (flag) *flag = st.flag;
   if (n_edges) *n_edges = st.n_edges;
   if (n_nodes) *n_nodes = st.n_nodes;
   if (scale) *scale = st.scale;
   if (st.n_edges > 0) {
-    if (ea) CK(cudaMemcpyAsync(ea, h->b.ea, sizeof(int32_t) * st.n_edges, cudaMemcpyDeviceToHost, h->stream));
-    if (eb) CK(cudaMemcpyAsync(eb, h->b.eb, sizeof(int32_t) * st.n_edges, cudaMemcpyDeviceToHost, h->stream));
-    if (ey) CK(cudaMemcpyAsync(ey, h->b.ey, st.n_edges, cudaMemcpyDeviceToHost, h->stream));
+    if (ea) CK(cudaMemcpyAsync(ea, bl.ea, sizeof(int32_t) * st.n_edges, cudaMemcpyDeviceToHost, h->stream));
+    if (eb) CK(cudaMemcpyAsync(eb, bl.eb, sizeof(int32_t) * st.n_edges, cudaMemcpyDeviceToHost, h->stream));
+    if (ey) CK(cudaMemcpyAsync(ey, bl.ey, st.n_edges, cudaMemcpyDeviceToHost, h->stream));
   }
   if (st.n_nodes > 0) {
-    if (nodes) CK(cudaMemcpyAsync(nodes, h->b.nodes, sizeof(int32_t) * st.n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    if (nodes) CK(cudaMemcpyAsync(nodes, bl.nodes, sizeof(int32_t) * st.n_nodes, cudaMemcpyDeviceToHost, h->stream));
     if (nbrs || nbr_y) {
       std::vector<uint32_t> packed((size_t)st.n_nodes * h->m.n_out);
-      CK(cudaMemcpyAsync(packed.data(), h->b.nbr, sizeof(uint32_t) * packed.size(), cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaMemcpyAsync(packed.data(), bl.nbr, sizeof(uint32_t) * packed.size(), cudaMemcpyDeviceToHost, h->stream));
       CK(cudaStreamSynchronize(h->stream));
       for (size_t q = 0; q < packed.size(); ++q) {
         if (nbrs) nbrs[q] = (int32_t)(packed[q] & 0x7fffffffu);
@@ -901,9 +979,9 @@ int ammsb_get_last_minibatch(ammsb_handle* h, int32_t* flag, int32_t* n_edges, i
     }
   }
   CK(cudaStreamSynchronize(h->stream));
-  if (st.err) {
-    h->err = "device sampling error bits " + std::to_string(st.err);
-    return (st.err & kErrCapacity) ? AMMSB_E_CAPACITY : AMMSB_E_SAMPLING;
+  if (gc.err) {
+    h->err = "device error bits " + std::to_string(gc.err);
+    return (gc.err & kErrCapacity) ? AMMSB_E_CAPACITY : AMMSB_E_SAMPLING;
   }
   return AMMSB_OK;
 }
@@ -933,18 +1011,21 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
     return AMMSB_E_STATE;
   }
   CK(cudaSetDevice(h->device));
+  int rc0 = invalidate_prefetch(h);
+  if (rc0) return rc0;
+  const Buffers& bp = h->bufs[h->parity];
   cudaEvent_t ev[6];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaEventRecord(ev[0], h->stream));
-  k_sample_minibatch<<<1, 1024, 0, h->stream>>>(h->m, h->g, h->b);
+  k_sample_minibatch<<<1, 1024, 0, h->stream>>>(h->m, h->g, bp);
   CK(cudaEventRecord(ev[1], h->stream));
-  k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, h->stream>>>(h->m, h->g, h->b);
+  k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, h->stream>>>(h->m, h->g, bp);
   CK(cudaEventRecord(ev[2], h->stream));
-  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_phi<__nv_bfloat16>(h, h->b) : launch_phi<float>(h, h->b));
+  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_phi<__nv_bfloat16>(h, bp) : launch_phi<float>(h, bp));
   CK(cudaEventRecord(ev[3], h->stream));
-  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_commit<__nv_bfloat16>(h, h->b) : launch_commit<float>(h, h->b));
+  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_commit<__nv_bfloat16>(h, bp) : launch_commit<float>(h, bp));
   CK(cudaEventRecord(ev[4], h->stream));
-  k_theta<<<(h->m.K + 31) / 32, 256, 0, h->stream>>>(h->m, h->b);
+  k_theta<<<(h->m.K + 31) / 32, 256, 0, h->stream>>>(h->m, bp);
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[5], h->stream));
   CK(cudaEventSynchronize(ev[5]));
@@ -955,6 +1036,7 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
   }
   for (auto& e : ev) cudaEventDestroy(e);
   h->step_count += 1;
+  h->last = h->parity;
   return check_device_err(h);
 }
 
@@ -963,11 +1045,11 @@ void* ammsb_stream(ammsb_handle* h) { return h ? (void*)h->stream : nullptr; }
 int ammsb_get_counters(ammsb_handle* h, uint64_t* edge_evals, uint64_t* iterations) {
   if (!h) return AMMSB_E_ARG;
   CK(cudaSetDevice(h->device));
-  DevState st;
-  CK(cudaMemcpyAsync(&st, h->b.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  DevCounters gc;
+  CK(cudaMemcpyAsync(&gc, h->gc, sizeof(gc), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  if (edge_evals) *edge_evals = st.evals;
-  if (iterations) *iterations = st.iters;
+  if (edge_evals) *edge_evals = gc.evals;
+  if (iterations) *iterations = gc.iters;
   return AMMSB_OK;
 }
 

@@ -53,7 +53,8 @@ struct Buffers {
   float* beta_part;    // nbb x 2 x Kp
   const float* fed_phi_noise;    // max_nodes x K or null
   const float* fed_theta_noise;  // K x 2 or null
-  DevState* st;
+  DevState* st;        // this buffer set's per-iteration scalars
+  DevCounters* gc;     // sampler-wide counters
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -117,9 +118,9 @@ __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, 
   const int tid = threadIdx.x;
   const Stream rs{m.seed, m.chain};
   if (tid == 0) {
-    const uint32_t step = b.st->next_step;
+    const uint32_t step = b.gc->next_step;
     b.st->step = step;
-    b.st->next_step = step + 1;
+    b.gc->next_step = step + 1;
     b.st->eps = eps_schedule(m.a, m.b, m.c, step);
     int flag;
     if (m.strategy == 0)
@@ -254,11 +255,7 @@ __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, 
     b.st->n_edges = s_count;
     b.st->n_nodes = err ? 0 : s_count + 1;
     b.st->rounds = rounds;
-    if (!err) {
-      b.st->evals += (unsigned long long)(s_count + 1) * (unsigned long long)m.n_out;
-      b.st->iters += 1ull;
-    }
-    if (err) atomicOr(&b.st->err, err);
+    if (err) atomicOr(&b.gc->err, err);
   }
 }
 
@@ -283,7 +280,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
     uint64_t t = 0;
     while (count < m.n_out) {
       if (t >= cap) {
-        if (lane == 0) atomicOr(&b.st->err, kErrNeighborCap);
+        if (lane == 0) atomicOr(&b.gc->err, kErrNeighborCap);
         break;
       }
       const int32_t j = (int32_t)(rs.draw_u64(kTagNbr, (uint32_t)i, step, t + lane) % (uint64_t)g.n);
@@ -421,9 +418,10 @@ __global__ void __launch_bounds__(NPB * SPLIT * LPN)
         float x[EPL];
 #pragma unroll
         for (int v = 0; v < VPL; ++v) TR::unpack(cur[v], x + v * EV);
-        float D = 0.f;
+        float d4[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int e = 0; e < EPL; ++e) D = fmaf(w[e], x[e], D);
+        for (int e = 0; e < EPL; ++e) d4[e & 3] = fmaf(w[e], x[e], d4[e & 3]);
+        float D = (d4[0] + d4[1]) + (d4[2] + d4[3]);
 #pragma unroll
         for (int o = LPN / 2; o > 0; o >>= 1) D += __shfl_xor_sync(gmask, D, o);
         const bool y = (wcur >> 31) != 0;
@@ -661,6 +659,10 @@ __global__ void __launch_bounds__(256) k_theta(Model m, Buffers b) {
   const uint32_t step = b.st->step;
   const double eps_t = (double)b.st->eps;
   const double scale = (double)b.st->scale;
+  if (k == 0) {  // the iteration's edge evaluations, counted once it is applied
+    b.gc->evals += (unsigned long long)b.st->n_nodes * (unsigned long long)m.n_out;
+    b.gc->iters += 1ull;
+  }
   const double th0 = b.theta[2 * k], th1 = b.theta[2 * k + 1];
   const double ts_inv = 1.0 / (th0 + th1);
   const double bt = (double)b.beta[k];

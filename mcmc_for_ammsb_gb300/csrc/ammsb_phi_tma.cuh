@@ -89,7 +89,7 @@ struct PhiTmaSmem {
 };
 
 template <typename PiT, int VPL, int SPLIT, int STAGES>
-__global__ void __launch_bounds__(SPLIT * 32) k_update_phi_tma(Model m, Buffers b) {
+__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1) k_update_phi_tma(Model m, Buffers b) {
   using TR = PiTraits<PiT>;
   constexpr int EV = TR::kPerVec;
   constexpr int EPL = VPL * EV;
@@ -187,17 +187,20 @@ __global__ void __launch_bounds__(SPLIT * 32) k_update_phi_tma(Model m, Buffers 
         break;
       }
       const PiT* row = my_ring + (size_t)stg * Kp;
-      float D = 0.f;
+      // the lane's slice of the row, unpacked once for both FMA passes
+      float x[EPL];
 #pragma unroll
       for (int v = 0; v < VPL; ++v) {
         const int vi = lane + 32 * v;
-        if (vi < nvec) {
-          float x[EV];
-          TR::unpack(*reinterpret_cast<const uint4*>(row + vi * EV), x);
-#pragma unroll
-          for (int e = 0; e < EV; ++e) D = fmaf(w[v * EV + e], x[e], D);
-        }
+        const uint4 raw = (vi < nvec) ? *reinterpret_cast<const uint4*>(row + vi * EV)
+                                      : make_uint4(0, 0, 0, 0);
+        TR::unpack(raw, x + v * EV);
       }
+      // four independent partial sums break the FMA dependency chain
+      float d4[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int e = 0; e < EPL; ++e) d4[e & 3] = fmaf(w[e], x[e], d4[e & 3]);
+      float D = (d4[0] + d4[1]) + (d4[2] + d4[3]);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) D += __shfl_xor_sync(0xffffffffu, D, o);
       const uint32_t word = s_nb[warp + SPLIT * t];
@@ -209,15 +212,7 @@ __global__ void __launch_bounds__(SPLIT * 32) k_update_phi_tma(Model m, Buffers 
       const float cj = sgn * invP;
       Bsum += (ej * one_m_si - sgn * D) * invP;
 #pragma unroll
-      for (int v = 0; v < VPL; ++v) {
-        const int vi = lane + 32 * v;
-        if (vi < nvec) {
-          float x[EV];
-          TR::unpack(*reinterpret_cast<const uint4*>(row + vi * EV), x);
-#pragma unroll
-          for (int e = 0; e < EV; ++e) A[v * EV + e] = fmaf(cj, x[e], A[v * EV + e]);
-        }
-      }
+      for (int e = 0; e < EPL; ++e) A[e] = fmaf(cj, x[e], A[e]);
       __syncwarp();
       if (lane == 0 && t + STAGES < T) {  // refill this stage with row t + STAGES
         const uint32_t j = s_nb[warp + SPLIT * (t + STAGES)] & 0x7fffffffu;
@@ -235,7 +230,7 @@ __global__ void __launch_bounds__(SPLIT * 32) k_update_phi_tma(Model m, Buffers 
         mbar_wait_bounded(my_bars + sq % STAGES, (sq / STAGES) & 1u);
       }
       if (lane == 0) {
-        atomicOr(&b.st->err, kErrPipeline);
+        atomicOr(&b.gc->err, kErrPipeline);
         s_broken = 1;
       }
     }

@@ -32,27 +32,6 @@ def rel_err(a, b, floor=1e-30):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if a.size else 0.0
 
 
-def phi_terms(net, resolved, phi, theta, mb, nbrs, nby, pn, step):
-    """FP64 magnitude of the terms that make up each new phi element,
-    |phi| + |eps/2 (alpha - phi + Nn grad)| + |sqrt(eps phi) noise|: the
-    scale against which a cancelling update's rounding is measured."""
-    K = phi.shape[1]
-    phi64 = phi.astype(np.float64)
-    pi64 = oracle.normalize(phi64, np.float64)
-    th = theta.astype(np.float64)
-    beta = th[:, 1] / th.sum(1)
-    eps = float(oracle.eps_t(resolved.a, resolved.b, resolved.c, step))
-    Nn = net.N / resolved.num_node_sample
-    M = np.zeros((len(mb["nodes"]), K))
-    for r, node in enumerate(mb["nodes"]):
-        g = oracle.phi_grad(K, pi64, phi64[node], int(node), nbrs[r], nby[r], beta,
-                            resolved.epsilon)
-        p = phi64[node]
-        M[r] = np.abs(p) + eps / 2 * np.abs(resolved.alpha - p + Nn * g) + \
-            np.abs(np.sqrt(eps * p) * pn[r])
-    return M
-
-
 def check_phi(got, f32, f64, M, tol=RTOL_STEP):
     """New phi rows against the oracle: element by element within tol of
     the update's term magnitude plus twice the float restatement's own
@@ -153,33 +132,26 @@ def test_sampling_small_population_collisions(native_lib):
 # ---------------------------------------------------------------------------
 # one fed step: update_phi + pi + update_beta against the literal oracle
 # ---------------------------------------------------------------------------
-def fed_inputs(net, s, opts, step, seed=0):
-    og = oracle.OracleGraph(net)
-    mb = oracle.sample_minibatch(og, 0, s.resolved.mini_batch_size, net.num_total_edges,
-                                 opts.random_seed, 0, step, s.max_edges)
-    n_out = s.num_node_sample + 1
-    nbrs = np.zeros((len(mb["nodes"]), n_out), np.int32)
-    nby = np.zeros_like(nbrs, dtype=np.uint8)
-    for r, node in enumerate(mb["nodes"]):
-        nbrs[r], nby[r] = oracle.sample_neighbors(og, int(node), n_out, opts.random_seed, 0, step)
-    rng = np.random.default_rng(seed)
-    pn = rng.standard_normal((len(mb["nodes"]), s.K)).astype(np.float32)
-    tn = rng.standard_normal((s.K, 2)).astype(np.float32)
-    return mb, nbrs, nby, pn, tn
-
-
-def oracle_fed_step(net, opts, resolved, phi, theta, mb, nbrs, nby, pn, tn, step, dtype):
+def oracle_fed_step(net, opts, resolved, phi, theta, mb, nbrs, nby, pn, tn, step, dtype,
+                    pi_nbr=None):
+    """The fed step through the literal oracle.  Neighbour rows of pi are
+    `pi_nbr` (the device's stored pi, e.g. BF16 values) when given; a node's
+    own pi row is phi_i / sum(phi_i), as the kernel computes it."""
     K = phi.shape[1]
     phi = phi.astype(dtype)
-    pi = oracle.normalize(phi, dtype)
+    pi = oracle.normalize(phi, dtype) if pi_nbr is None else pi_nbr.astype(dtype).copy()
+    own = oracle.normalize(phi[mb["nodes"]], dtype)
     th = theta.astype(dtype)
-    beta = (th[:, 1] / (th[:, 0] + th[:, 1])).astype(dtype)
+    beta = (th[:, 1] / (th[:, 0] + th[:, 1])).astype(np.float32).astype(dtype)
     eps = oracle.eps_t(resolved.a, resolved.b, resolved.c, step)
     new_phi = phi.copy()
     for r, node in enumerate(mb["nodes"]):
+        keep = pi[node].copy()
+        pi[node] = own[r]
         new_phi[node] = oracle.update_phi(K, pi, phi[node], int(node), nbrs[r], nby[r], beta,
                                           resolved.alpha, resolved.epsilon, eps, net.N,
                                           resolved.num_node_sample, pn[r], dtype)
+        pi[node] = keep
     new_pi = pi.copy()
     idx = mb["nodes"]
     new_pi[idx] = oracle.normalize(new_phi[idx], dtype)
@@ -191,119 +163,133 @@ def oracle_fed_step(net, opts, resolved, phi, theta, mb, nbrs, nby, pn, tn, step
     return new_phi, new_pi, th2, bt2
 
 
-@pytest.mark.parametrize("K", [32, 20])
-@pytest.mark.parametrize("step", [1, 37])
-def test_fed_step_matches_oracle_f32(small, K, step):
-    net, _ = small
-    s, opts = make_sampler(net, K=K)
+def phi_terms(net, resolved, phi, theta, mb, nbrs, nby, pn, step, pi_nbr=None):
+    """FP64 magnitude of the terms that make up each new phi element,
+    |phi| + |eps/2 (alpha - phi + Nn grad)| + |sqrt(eps phi) noise|: the
+    scale against which a cancelling update's rounding is measured."""
+    K = phi.shape[1]
+    phi64 = phi.astype(np.float64)
+    pi64 = oracle.normalize(phi64, np.float64) if pi_nbr is None else pi_nbr.astype(np.float64)
+    own = oracle.normalize(phi64[mb["nodes"]], np.float64)
+    th = theta.astype(np.float64)
+    beta = th[:, 1] / th.sum(1)
+    eps = float(oracle.eps_t(resolved.a, resolved.b, resolved.c, step))
+    Nn = net.N / resolved.num_node_sample
+    M = np.zeros((len(mb["nodes"]), K))
+    for r, node in enumerate(mb["nodes"]):
+        keep = pi64[node].copy()
+        pi64[node] = own[r]
+        g = oracle.phi_grad(K, pi64, phi64[node], int(node), nbrs[r], nby[r], beta,
+                            resolved.epsilon)
+        pi64[node] = keep
+        p = phi64[node]
+        M[r] = np.abs(p) + eps / 2 * np.abs(resolved.alpha - p + Nn * g) + \
+            np.abs(np.sqrt(eps * p) * pn[r])
+    return M
+
+
+def check_theta(s, K, theta, mb, tn, step, want_th, want_bt, f_th, f_bt):
+    """theta/beta are FP64 on the device.  Isolated: update_beta on the
+    device's own new pi (its phi rows normalised) matches the FP64 oracle to
+    1e-6; end to end within 1e-4 of the FP64 chain and within the float
+    restatement's own rounding (2x its distance to FP64) of the float chain."""
+    new_pi = oracle.normalize(s.phi.astype(np.float64), np.float64)
+    th64 = theta.astype(np.float64)
+    bt_dev = (th64[:, 1] / th64.sum(1)).astype(np.float32).astype(np.float64)
+    eps = oracle.eps_t(s.resolved.a, s.resolved.b, s.resolved.c, step)
+    iso_th, _, _ = oracle.update_beta(
+        K, new_pi, mb["nodes"][mb["edge_a"]], mb["nodes"][mb["edge_b"]], mb["edge_y"], th64,
+        bt_dev, np.array([s.resolved.eta0, s.resolved.eta1]), s.resolved.epsilon, eps,
+        mb["scale"], tn, np.float64)
+    gth = s.theta
+    assert rel_err(gth, iso_th) < 1e-6
+    assert rel_err(gth, f_th) < RTOL_F64
+    assert rel_err(gth, want_th) < max(RTOL_STEP, 2 * rel_err(want_th, f_th))
+    assert rel_err(s.beta, want_bt) < max(RTOL_STEP, 2 * rel_err(want_bt, f_bt))
+
+
+def run_fed_case(net, K, step, dtype, strategy=0, mini_batch_size=None, num_node_sample=32):
+    kw = dict(K=K, num_node_sample=num_node_sample)
+    if mini_batch_size:
+        kw["mini_batch_size"] = mini_batch_size
+    s, opts = make_sampler(net, dtype, **kw)
     phi, theta = random_state(net.N, K, seed=step)
     s.set_state(phi, theta)
-    mb, nbrs, nby, pn, tn = fed_inputs(net, s, opts, step)
-    s.step_fed(step, np.stack([mb["edge_a"], mb["edge_b"]], 1), mb["edge_y"], mb["scale"],
-               mb["nodes"], nbrs, nby, pn, tn)
-    want_phi, want_pi, want_th, want_bt = oracle_fed_step(net, opts, s.resolved, phi, theta, mb,
-                                                          nbrs, nby, pn, tn, step, np.float32)
-    idx = mb["nodes"]
-    f_phi, f_pi, f_th, f_bt = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby,
-                                              pn, tn, step, np.float64)
-    M = phi_terms(net, s.resolved, phi, theta, mb, nbrs, nby, pn, step)
-    gphi = s.phi
-    check_phi(gphi[idx], want_phi[idx], f_phi[idx], M)
-    gpi = s.pi
-    assert np.all(np.linalg.norm(gpi[idx] - want_pi[idx], axis=1) /
-                  np.linalg.norm(want_pi[idx], axis=1) < RTOL_STEP)
-    untouched = np.setdiff1d(np.arange(net.N), idx)
-    assert np.array_equal(gphi[untouched], phi[untouched])
-    # theta/beta are FP64 on the device.  Isolated: update_beta on the
-    # device's own new pi must match the FP64 oracle to 1e-6.
-    gpu_pi = s.pi.astype(np.float64)
-    th64 = theta.astype(np.float64)
-    bt_dev = (th64[:, 1] / th64.sum(1)).astype(np.float32).astype(np.float64)  # device beta
-    eps = oracle.eps_t(s.resolved.a, s.resolved.b, s.resolved.c, step)
-    iso_th, iso_bt, _ = oracle.update_beta(
-        K, gpu_pi, mb["nodes"][mb["edge_a"]], mb["nodes"][mb["edge_b"]], mb["edge_y"], th64,
-        bt_dev, np.array([1.0, 1.0]), s.resolved.epsilon, eps, mb["scale"], tn, np.float64)
-    assert rel_err(s.theta, iso_th) < 1e-6
-    # end to end the float phi error propagates: within the FP64 tolerance of
-    # the FP64 chain, and within the float restatement's own rounding (2x its
-    # distance to FP64) of the float chain
-    assert rel_err(s.theta, f_th) < RTOL_F64
-    assert rel_err(s.theta, want_th) < max(RTOL_STEP, 2 * rel_err(want_th, f_th))
-    assert rel_err(s.beta, want_bt) < max(RTOL_STEP, 2 * rel_err(want_bt, f_bt))
-    s.close()
-
-
-def test_fed_step_link_stratum(small):
-    """A link-stratum (y = 1) minibatch through the fed path."""
-    net, _ = small
-    s, opts = make_sampler(net, strategy=1)
-    phi, theta = random_state(net.N, 32, seed=3)
-    s.set_state(phi, theta)
+    pi_dev = s.pi  # the stored pi the kernel gathers neighbour rows from
     og = oracle.OracleGraph(net)
-    mb = oracle.sample_minibatch(og, 1, s.resolved.mini_batch_size, net.num_total_edges,
-                                 opts.random_seed, 0, 5, s.max_edges)
-    assert mb["flag"] == 1 and mb["edge_y"].all()
+    mb = oracle.sample_minibatch(og, strategy, s.resolved.mini_batch_size, net.num_total_edges,
+                                 opts.random_seed, 0, step, s.max_edges)
     n_out = s.num_node_sample + 1
     nbrs = np.zeros((len(mb["nodes"]), n_out), np.int32)
     nby = np.zeros_like(nbrs, dtype=np.uint8)
     for r, node in enumerate(mb["nodes"]):
-        nbrs[r], nby[r] = oracle.sample_neighbors(og, int(node), n_out, 42, 0, 5)
-    rng = np.random.default_rng(1)
-    pn = rng.standard_normal((len(mb["nodes"]), 32)).astype(np.float32)
-    tn = rng.standard_normal((32, 2)).astype(np.float32)
-    s.step_fed(5, np.stack([mb["edge_a"], mb["edge_b"]], 1), mb["edge_y"], mb["scale"],
+        nbrs[r], nby[r] = oracle.sample_neighbors(og, int(node), n_out, opts.random_seed, 0, step)
+    rng = np.random.default_rng(step)
+    pn = rng.standard_normal((len(mb["nodes"]), K)).astype(np.float32)
+    tn = rng.standard_normal((K, 2)).astype(np.float32)
+    s.step_fed(step, np.stack([mb["edge_a"], mb["edge_b"]], 1), mb["edge_y"], mb["scale"],
                mb["nodes"], nbrs, nby, pn, tn)
-    want_phi, want_pi, want_th, want_bt = oracle_fed_step(net, opts, s.resolved, phi, theta, mb,
-                                                          nbrs, nby, pn, tn, 5, np.float32)
-    f_phi, _, f_th, _ = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby, pn, tn,
-                                        5, np.float64)
-    M = phi_terms(net, s.resolved, phi, theta, mb, nbrs, nby, pn, 5)
-    check_phi(s.phi[mb["nodes"]], want_phi[mb["nodes"]], f_phi[mb["nodes"]], M)
-    assert rel_err(s.theta, f_th) < RTOL_F64
-    assert rel_err(s.theta, want_th) < max(RTOL_STEP, 2 * rel_err(want_th, f_th))
+    want = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby, pn, tn, step,
+                           np.float32, pi_dev)
+    f64 = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby, pn, tn, step,
+                          np.float64, pi_dev)
+    M = phi_terms(net, s.resolved, phi, theta, mb, nbrs, nby, pn, step, pi_dev)
+    idx = mb["nodes"]
+    gphi = s.phi
+    check_phi(gphi[idx], want[0][idx], f64[0][idx], M)
+    untouched = np.setdiff1d(np.arange(net.N), idx)
+    assert np.array_equal(gphi[untouched], phi[untouched])
+    gpi = s.pi
+    if dtype == _native.PI_F32:
+        assert np.all(np.linalg.norm(gpi[idx] - want[1][idx], axis=1) /
+                      np.linalg.norm(want[1][idx], axis=1) < RTOL_STEP)
+    else:  # committed rows are the BF16 rounding of the FP32 new pi
+        assert np.all(np.abs(gpi[idx] - f64[1][idx]) <= 2.0 ** -8 * np.abs(f64[1][idx]) + 1e-30)
+    assert np.array_equal(gpi[untouched], pi_dev[untouched])
+    check_theta(s, K, theta, mb, tn, step, want[2], want[3], f64[2], f64[3])
     s.close()
+    return mb
 
 
-@pytest.mark.parametrize("K", [1024, 256, 200])
-def test_fed_step_wide_rows(native_lib, K):
-    """Wide-row kernels: the bulk-copy pipeline (K >= 256 BF16, >= 128 F32)
-    and its padded-row case (K = 200)."""
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+@pytest.mark.parametrize("K", [32, 20])
+@pytest.mark.parametrize("step", [1, 37])
+def test_fed_step_matches_oracle(small, K, step, dtype):
+    net, _ = small
+    run_fed_case(net, K, step, dtype)
+
+
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+def test_fed_step_link_stratum(small, dtype):
+    """A link-stratum (y = 1) minibatch through the fed path."""
+    net, _ = small
+    mb = run_fed_case(net, 32, 5, dtype, strategy=1)
+    assert mb["flag"] == 1 and mb["edge_y"].all()
+
+
+@pytest.fixture(scope="module")
+def wide_net(native_lib):
     net = Network.synthetic(n=3000, k_true=30, intra_degree=6.0, seed=4)
     net.make_held_out(0.02, seed=4)
-    for dtype in (_native.PI_F32, _native.PI_BF16):
-        s, opts = make_sampler(net, dtype, K=K, num_node_sample=40, mini_batch_size=64)
-        phi, theta = random_state(net.N, K, seed=2)
-        s.set_state(phi, theta)
-        mb, nbrs, nby, pn, tn = fed_inputs(net, s, opts, 3)
-        s.step_fed(3, np.stack([mb["edge_a"], mb["edge_b"]], 1), mb["edge_y"], mb["scale"],
-                   mb["nodes"], nbrs, nby, pn, tn)
-        idx = mb["nodes"]
-        if dtype == _native.PI_F32:
-            want_phi, _, want_th, _ = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs,
-                                                      nby, pn, tn, 3, np.float32)
-            f_phi, _, _, _ = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby,
-                                             pn, tn, 3, np.float64)
-            M = phi_terms(net, s.resolved, phi, theta, mb, nbrs, nby, pn, 3)
-            check_phi(s.phi[idx], want_phi[idx], f_phi[idx], M)
-            f_phi, _, f_th, _ = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby,
-                                                pn, tn, 3, np.float64)
-            assert rel_err(s.theta, f_th) < RTOL_F64
-        else:
-            # BF16 neighbour rows: the step against the f64 oracle on the
-            # BF16-rounded pi is the meaningful comparison
-            f_phi, _, f_th, _ = oracle_fed_step(net, opts, s.resolved, phi, theta, mb, nbrs, nby,
-                                                pn, tn, 3, np.float64)
-            assert rel_err(s.phi[idx], f_phi[idx]) < 5e-3
-        s.close()
+    return net
+
+
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+@pytest.mark.parametrize("K", [1024, 256, 200, 64])
+def test_fed_step_wide_rows(wide_net, K, dtype):
+    """Wide-row kernels: the bulk-copy pipeline (rows of >= 32 vectors),
+    padded rows (K = 200) and the sub-warp register path (K = 64 BF16)."""
+    run_fed_case(wide_net, K, 3, dtype, mini_batch_size=64, num_node_sample=40)
 
 
 # ---------------------------------------------------------------------------
 # perplexity
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("K", [32, 24])
-def test_perplexity_matches_oracle(small, K):
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+@pytest.mark.parametrize("K", [32, 24, 1024])
+def test_perplexity_matches_oracle(small, K, dtype):
     net, _ = small
-    s, opts = make_sampler(net, K=K)
+    s, opts = make_sampler(net, dtype, K=K)
     phi, theta = random_state(net.N, K, seed=11)
     s.set_state(phi, theta)
     pi = s.pi
