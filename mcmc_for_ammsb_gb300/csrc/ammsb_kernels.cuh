@@ -111,7 +111,7 @@ __device__ __forceinline__ int block_scan_1024(bool flag, int* s_warp, int* tota
 // (atomicMin of its index in a hash), then an ordered block scan appends
 // them -- exactly the sequential scan of the oracle.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, Buffers b) {
+static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, Buffers b) {
   __shared__ int s_warp[33];
   __shared__ int s_flag, s_count;
   __shared__ uint32_t s_step;
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int nco
 //   G_k0 = beta R1 (0 - 1/ts) + (1-beta) R0 (1/theta_k0 - 1/ts)
 //   G_k1 = beta R1 (1/theta_k1 - 1/ts) + (1-beta) R0 (0 - 1/ts)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_theta(Model m, Buffers b) {
+static __global__ void __launch_bounds__(256) k_theta(Model m, Buffers b) {
   // 32 consecutive k per CTA; warp w sums block partials w, w+8, ... in FP64,
   // then warp 0 adds the eight warp sums in fixed order (deterministic).
   __shared__ double s_r0[8][32], s_r1[8][32];
@@ -769,7 +769,7 @@ __global__ void __launch_bounds__(256) k_perplexity(Model m, const PiT* __restri
   }
 }
 
-__global__ void k_ppx_final(const double* part, int nblk, int64_t H, double* out) {
+static __global__ void k_ppx_final(const double* part, int nblk, int64_t H, double* out) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double t = 0.0, c = 0.0;
   for (int q = 0; q < nblk; ++q) {
@@ -784,7 +784,7 @@ __global__ void k_ppx_final(const double* part, int nblk, int64_t H, double* out
 // ---------------------------------------------------------------------------
 // init: phi ~ Gamma(1,1) (cc:66), row normalisation into pi (cc:75)
 // ---------------------------------------------------------------------------
-__global__ void k_init_phi(Model m, float* phi, double shape, double scale, int32_t* err) {
+static __global__ void k_init_phi(Model m, float* phi, double shape, double scale, int32_t* err) {
   const Stream rs{m.seed, m.chain};
   const int64_t total = m.N * (int64_t)m.Kp;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total;

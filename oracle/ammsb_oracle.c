@@ -160,6 +160,12 @@ float oracle_eps_t(double a, double b, double c, uint64_t step) {
   return (float)(a * pow(1.0 + (double)step / b, -c));
 }
 
+/* get_eps_t as the reference evaluates it with Float = float
+ * (mcmc_sampler_stochastic.h:112-115): step_count / b in float, powf. */
+float oracle_eps_t_ref(float a, float b, float c, uint64_t step) {
+  return a * powf(1.0f + (float)step / b, -c);
+}
+
 #define NONLINK_CAND_CAP(m) (64 * (int64_t)(m) + 4096)
 #define LINK_ATTEMPT_CAP 4096
 

@@ -102,6 +102,8 @@ float oracle_nonlink_scale(int64_t N, int64_t m, int64_t num_total_edges);
 /* eps_t = a (1 + t/b)^-c (mcmc_sampler_stochastic.h:112-115), in double then
  * rounded to float. */
 float oracle_eps_t(double a, double b, double c, uint64_t step);
+/* the reference's own float evaluation of the same formula */
+float oracle_eps_t_ref(float a, float b, float c, uint64_t step);
 
 /* ---- hot-path arithmetic, literal restatements --------------------------*/
 /* update_phi for one node (mcmc_sampler_stochastic.cc:269-313).

@@ -70,6 +70,8 @@ def lib():
         L.oracle_nonlink_scale.argtypes = [ctypes.c_int64] * 3
         L.oracle_eps_t.restype = ctypes.c_float
         L.oracle_eps_t.argtypes = [ctypes.c_double] * 3 + [ctypes.c_uint64]
+        L.oracle_eps_t_ref.restype = ctypes.c_float
+        L.oracle_eps_t_ref.argtypes = [ctypes.c_float] * 3 + [ctypes.c_uint64]
         L.oracle_sample_minibatch.restype = ctypes.c_int
         L.oracle_sample_neighbors.restype = ctypes.c_int64
         L.oracle_edge_likelihood_f32.restype = ctypes.c_float
@@ -151,6 +153,10 @@ def normals(seed, chain, tag, entity, step, count):
 
 def eps_t(a, b, c, step):
     return lib().oracle_eps_t(a, b, c, step)
+
+
+def eps_t_ref(a, b, c, step):
+    return lib().oracle_eps_t_ref(a, b, c, step)
 
 
 def nonlink_scale(N, m, E):

@@ -414,3 +414,54 @@ def test_errors(small):
         s.step(1)
     assert e.value.code == -5
     s.close()
+
+
+# ---------------------------------------------------------------------------
+# the CUDA path against the reference's own outputs (tests/golden/ref_*.npz)
+# ---------------------------------------------------------------------------
+import glob as _glob
+import os as _os
+
+_FIXTURES = sorted(_glob.glob(_os.path.join(_os.path.dirname(_os.path.abspath(__file__)),
+                                            "golden", "ref_*.npz")))
+
+
+@pytest.mark.parametrize("path", _FIXTURES, ids=[_os.path.basename(p) for p in _FIXTURES])
+def test_gpu_against_reference_fixture(native_lib, path):
+    d = dict(np.load(path))
+    N, K, nns = int(d["N"]), int(d["K"]), int(d["nns"])
+    net = Network.from_edges(N, d["edge_a"], d["edge_b"])
+    net.held_out = (d["ho_a"], d["ho_b"], d["ho_y"])
+    net.test = (d["te_a"], d["te_b"], d["te_y"])
+    E = set(zip(d["edge_a"].tolist(), d["edge_b"].tolist()))
+    opts = Options(K=K, num_node_sample=nns, mini_batch_size=int(d["mbs"]), a=float(d["a"]),
+                   b=float(d["b"]), c=float(d["c"]), alpha=float(np.float32(d["alpha"])),
+                   epsilon=float(d["epsilon"]))
+    s = MCMCSamplerStochastic(opts, net).create()
+    # update_phi of the reference's nodes, neighbour sets and noise
+    s.set_state(d["phi"], d["theta"].astype(np.float64))
+    nodes = d["phi_nodes"]
+    nbrs = d["phi_order"]
+    nby = np.array([[(min(v, j), max(v, j)) in E for j in row] for v, row in zip(nodes, nbrs)],
+                   np.uint8)
+    s.step_fed(int(d["step"]), np.zeros((0, 2), np.int32), np.zeros(0, np.uint8), 1.0, nodes,
+               nbrs, nby, d["phi_noise"], np.zeros((K, 2), np.float32))
+    mb = dict(nodes=nodes)
+    f64 = np.zeros((len(nodes), K))
+    pi64 = d["pi"].astype(np.float64)
+    for r, v in enumerate(nodes):
+        f64[r] = oracle.update_phi(K, pi64, d["phi"][v], int(v), nbrs[r], nby[r],
+                                   d["beta"].astype(np.float64), float(d["alpha"]),
+                                   float(d["epsilon"]), float(d["eps"]), N, nns,
+                                   d["phi_noise"][r], np.float64)
+    M = phi_terms(net, s.resolved, d["phi"], d["theta"], mb, nbrs, nby, d["phi_noise"],
+                  int(d["step"]), d["pi"])
+    check_phi(s.phi[nodes], d["phi_out"], f64, M)
+    # perplexity on the reference's state after update_beta (beta_out)
+    s.set_state(d["phi"], d["theta_out"].astype(np.float64))
+    p1 = s.cal_perplexity_held_out()
+    p2 = s.cal_perplexity_held_out()
+    assert p1 == pytest.approx(float(d["ppx1"]), rel=RTOL_PPX)
+    assert p2 == pytest.approx(float(d["ppx2"]), rel=RTOL_PPX)
+    assert rel_err(s.ppx_per_heldout_edge, d["ppx_edges2"]) < RTOL_PPX
+    s.close()
