@@ -188,6 +188,29 @@ void *ammsb_stream(ammsb_handle *h);
 int ammsb_get_counters(ammsb_handle *h, uint64_t *edge_evals,
                        uint64_t *iterations);
 
+/* Held-out perplexity without any device allocation.  No counterpart in
+ * the reference: it serves callers that cannot call cudaMalloc (a host
+ * program whose runtime owns every device allocation, or that must not
+ * allocate after start-up) and hold the sampler state in device memory they
+ * obtained themselves.  Same kernel and result as ammsb_perplexity, but no
+ * handle: pi (row_stride elements per row, 16-byte aligned rows, F32 or
+ * BF16), beta, the held-out pairs and the running averages ppx (updated)
+ * are caller-owned device arrays; *out (host) receives -mean log of the
+ * running averages.  Its scratch is a fixed 256 KB __device__ array, so
+ * held_count is limited to 4,194,304 (AMMSB_E_CAPACITY beyond).  The array
+ * is shared by every call on a device and keeps the last call's contents:
+ * calls whose kernels overlap on the GPU race.  The first call on a device
+ * looks up the array's address with that device current -- make it before
+ * any stream capture.  Runs on `stream` (a cudaStream_t, 0 for the legacy
+ * default stream) and synchronises it before returning. */
+int ammsb_perplexity_noalloc(const void *pi, int32_t pi_dtype, int64_t K,
+                             int64_t row_stride, const float *beta,
+                             double epsilon, const int32_t *held_a,
+                             const int32_t *held_b, const uint8_t *held_y,
+                             int64_t held_count, float *ppx,
+                             uint64_t average_count, void *stream,
+                             double *out);
+
 /* ------------------------------------------------------------------------ */
 /* Host-side data preparation (no GPU use).                                 */
 /* ------------------------------------------------------------------------ */

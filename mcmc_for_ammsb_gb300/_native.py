@@ -128,6 +128,9 @@ SIGNATURES = [
     ("ammsb_profile_step", ctypes.c_int, [_P, _F64P]),
     ("ammsb_stream", _P, [_P]),
     ("ammsb_get_counters", ctypes.c_int, [_P, _U64P, _U64P]),
+    ("ammsb_perplexity_noalloc", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
+                                                _P, ctypes.c_double, _P, _P, _P, ctypes.c_int64,
+                                                _P, ctypes.c_uint64, _P, _F64P]),
     ("ammsb_generate_graph", ctypes.c_int, [ctypes.POINTER(AmmsbGenParams), ctypes.POINTER(_P)]),
     ("ammsb_graph_from_edges", ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _I32P, _I32P,
                                               ctypes.POINTER(_P)]),
