@@ -51,11 +51,33 @@ struct DevGraph {
   uint32_t excl_mask;
 };
 
+// Membership of b in a sorted row held in shared memory.
+__device__ __forceinline__ bool row_contains(const int32_t* row, int32_t deg, int32_t b) {
+  int32_t lo = 0, hi = deg;
+  while (lo < hi) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (row[mid] < b)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo < deg && row[lo] == b;
+}
+
 constexpr unsigned long long kEmptyKey = ~0ull;
 
 __host__ __device__ __forceinline__ unsigned long long pair_key(int32_t a, int32_t b) {
   uint32_t lo = (uint32_t)(a < b ? a : b), hi = (uint32_t)(a < b ? b : a);
   return ((unsigned long long)lo << 32) | hi;
+}
+
+__host__ __device__ __forceinline__ uint64_t hash64_full(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
 }
 
 __host__ __device__ __forceinline__ uint32_t hash64(unsigned long long k) {
@@ -89,7 +111,25 @@ __device__ __forceinline__ bool is_excluded(const DevGraph& g, int32_t a, int32_
   return false;
 }
 
-// Edge::in(NetworkGraph): binary search in the sorted row of a.
+// Finishes a linear-probing lookup whose first slot `slot` was already
+// loaded as `first` (so callers can issue several first loads at once).
+__device__ __forceinline__ bool probe_resolve(const unsigned long long* tab,
+                                              unsigned long long mask,
+                                              unsigned long long key,
+                                              unsigned long long slot,
+                                              unsigned long long first) {
+  if (first == key) return true;
+  if (first == kEmptyKey) return false;
+  for (unsigned long long probe = 1; probe <= mask; ++probe) {
+    slot = (slot + 1) & mask;
+    const unsigned long long k = __ldg(tab + slot);
+    if (k == key) return true;
+    if (k == kEmptyKey) return false;
+  }
+  return false;
+}
+
+// Edge::in(NetworkGraph) by binary search in the sorted row of a.
 __device__ __forceinline__ bool has_edge(const DevGraph& g, int32_t a, int32_t b) {
   int64_t lo = __ldg(g.row_ptr + a), hi = __ldg(g.row_ptr + a + 1);
   const int64_t end = hi;

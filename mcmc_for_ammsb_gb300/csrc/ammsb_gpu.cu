@@ -96,7 +96,7 @@ struct ammsb_handle {
   int32_t* d_err_init = nullptr;
   int ncommit = 1;
   int nbr_blocks = 1, phi_blocks = 1;
-  size_t phi_smem = 0, nbr_smem = 0;
+  size_t phi_smem = 0, nbr_smem = 0, mb_smem = 0;
   // host mirrors
   uint64_t step_count = 1;     // learner.cc:37
   uint64_t average_count = 1;  // learner.cc:30
@@ -232,13 +232,13 @@ cudaError_t launch_update_phase(ammsb_handle* h, const Buffers& b) {
   e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_commit<__nv_bfloat16>(h, b)
                                           : launch_commit<float>(h, b);
   if (e != cudaSuccess) return e;
-  k_theta<<<(h->m.K + 31) / 32, 256, 0, h->stream>>>(h->m, b);
+  k_theta<<<(h->m.K + 31) / 32, 1024, 0, h->stream>>>(h->m, b);
   return cudaGetLastError();
 }
 
 // Draws of one iteration (minibatch + neighbour sets) into buffer set b.
 cudaError_t launch_sampling_phase(ammsb_handle* h, const Buffers& b, cudaStream_t s) {
-  k_sample_minibatch<<<1, 1024, 0, s>>>(h->m, h->g, b);
+  k_sample_minibatch<<<1, 1024, h->mb_smem, s>>>(h->m, h->g, b, h->mb_smem > 0);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, s>>>(h->m, h->g, b);
@@ -584,6 +584,11 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   TRY(dev_alloc(h, &b.htab_key, (size_t)hcap));
   TRY(dev_alloc(h, &b.htab_idx, (size_t)hcap));
   b.hmask = (uint32_t)(hcap - 1);
+  // the dedup hash lives in shared memory when it fits (up to 16Ki entries)
+  if (hcap <= 16384 &&
+      cudaFuncSetAttribute(k_sample_minibatch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(2 * sizeof(uint32_t) * hcap)) == cudaSuccess)
+    h->mb_smem = 2 * sizeof(uint32_t) * (size_t)hcap;
   TRY(dev_alloc(h, &b.beta_part, (size_t)m.nbb * 2 * Kp));
   TRY(dev_alloc(h, &h->gc, 1));
   b.gc = h->gc;
@@ -1017,7 +1022,7 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
   cudaEvent_t ev[6];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaEventRecord(ev[0], h->stream));
-  k_sample_minibatch<<<1, 1024, 0, h->stream>>>(h->m, h->g, bp);
+  k_sample_minibatch<<<1, 1024, h->mb_smem, h->stream>>>(h->m, h->g, bp, h->mb_smem > 0);
   CK(cudaEventRecord(ev[1], h->stream));
   k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, h->stream>>>(h->m, h->g, bp);
   CK(cudaEventRecord(ev[2], h->stream));
@@ -1025,7 +1030,7 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
   CK(cudaEventRecord(ev[3], h->stream));
   CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_commit<__nv_bfloat16>(h, bp) : launch_commit<float>(h, bp));
   CK(cudaEventRecord(ev[4], h->stream));
-  k_theta<<<(h->m.K + 31) / 32, 256, 0, h->stream>>>(h->m, bp);
+  k_theta<<<(h->m.K + 31) / 32, 1024, 0, h->stream>>>(h->m, bp);
   CK(cudaGetLastError());
   CK(cudaEventRecord(ev[5], h->stream));
   CK(cudaEventSynchronize(ev[5]));

@@ -111,7 +111,11 @@ __device__ __forceinline__ int block_scan_1024(bool flag, int* s_warp, int* tota
 // (atomicMin of its index in a hash), then an ordered block scan appends
 // them -- exactly the sequential scan of the oracle.
 // ---------------------------------------------------------------------------
-static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, Buffers b) {
+static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, Buffers b,
+                                                                  int smem_hash) {
+  extern __shared__ uint32_t s_htab[];  // dedup hash in shared memory when it fits
+  constexpr int kRowCap = 2048;         // the source's row, staged when it fits
+  __shared__ int32_t s_row[kRowCap];
   __shared__ int s_warp[33];
   __shared__ int s_flag, s_count;
   __shared__ uint32_t s_step;
@@ -139,12 +143,19 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
   if (flag == 0) {
     const int mb = m.mini_batch_size;
     const int32_t v = (int32_t)(rs.draw_u64(kTagMbNode, 0, step, 0) % (uint64_t)g.n);
+    uint32_t* hkey = smem_hash ? s_htab : b.htab_key;
+    uint32_t* hidx = smem_hash ? s_htab + (b.hmask + 1) : b.htab_idx;
     for (uint32_t s = tid; s <= b.hmask; s += blockDim.x) {
-      b.htab_key[s] = 0xffffffffu;
-      b.htab_idx[s] = 0xffffffffu;
+      hkey[s] = 0xffffffffu;
+      hidx[s] = 0xffffffffu;
     }
     if (mb > m.max_edges || mb + 1 > m.max_nodes) err |= kErrCapacity;
     if (tid == 0) b.nodes[0] = v;
+    const int64_t vr0 = g.row_ptr[v];
+    const int32_t vdeg = (int32_t)(g.row_ptr[v + 1] - vr0);
+    const bool row_in_smem = vdeg <= kRowCap;
+    if (row_in_smem)
+      for (int q = tid; q < vdeg; q += blockDim.x) s_row[q] = g.col[vr0 + q];
     __syncthreads();
     int count = 0;
     uint64_t t = 0;
@@ -155,20 +166,44 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
         err |= kErrMinibatchCap;
         break;
       }
-      // pass A: validity and first-occurrence index per value
-      for (int c = tid; c < need; c += blockDim.x) {
-        const int32_t u = (int32_t)(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c) % (uint64_t)g.n);
-        const bool ok = (u != v) && !has_edge(g, v, u) && !is_excluded(g, v, u);
-        b.cand[c] = ok ? u : -1;
-        if (ok) {
-          uint32_t slot = hash32((uint32_t)u) & b.hmask;
-          for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
-            uint32_t prev = atomicCAS(b.htab_key + slot, 0xffffffffu, (uint32_t)u);
-            if (prev == 0xffffffffu || prev == (uint32_t)u) {
-              atomicMin(b.htab_idx + slot, (uint32_t)(t + (uint64_t)c));
-              break;
+      // pass A: validity and first-occurrence index per value; G candidates
+      // per thread with the first probes of both hashes issued together
+      constexpr int G = 4;
+      for (int c0 = tid; c0 < need; c0 += blockDim.x * G) {
+        int32_t u[G];
+        bool live[G];
+        unsigned long long key[G], xs[G], xk[G];
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+          const int c = c0 + j * blockDim.x;
+          live[j] = c < need;
+          u[j] = live[j] ? (int32_t)(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c) % (uint64_t)g.n)
+                         : -1;
+          live[j] = live[j] && (u[j] != v);
+          key[j] = pair_key(v, u[j] < 0 ? 0 : u[j]);
+          xs[j] = hash64(key[j]) & g.excl_mask;
+        }
+#pragma unroll
+        for (int j = 0; j < G; ++j) xk[j] = live[j] ? __ldg(g.excl + xs[j]) : kEmptyKey;
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+          const int c = c0 + j * blockDim.x;
+          if (c >= need) continue;
+          const bool linked = live[j] && (row_in_smem ? row_contains(s_row, vdeg, u[j])
+                                                      : has_edge(g, v, u[j]));
+          const bool ok = live[j] && !linked &&
+                          !probe_resolve(g.excl, g.excl_mask, key[j], xs[j], xk[j]);
+          b.cand[c] = ok ? u[j] : -1;
+          if (ok) {
+            uint32_t slot = hash32((uint32_t)u[j]) & b.hmask;
+            for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
+              const uint32_t prev = atomicCAS(hkey + slot, 0xffffffffu, (uint32_t)u[j]);
+              if (prev == 0xffffffffu || prev == (uint32_t)u[j]) {
+                atomicMin(hidx + slot, (uint32_t)(t + (uint64_t)c));
+                break;
+              }
+              slot = (slot + 1) & b.hmask;
             }
-            slot = (slot + 1) & b.hmask;
           }
         }
       }
@@ -183,9 +218,9 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
           if (u >= 0) {
             uint32_t slot = hash32((uint32_t)u) & b.hmask;
             for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
-              const uint32_t k = b.htab_key[slot];
+              const uint32_t k = hkey[slot];
               if (k == (uint32_t)u) {
-                acc = (b.htab_idx[slot] == (uint32_t)(t + (uint64_t)c));
+                acc = (hidx[slot] == (uint32_t)(t + (uint64_t)c));
                 break;
               }
               if (k == 0xffffffffu) break;
@@ -268,14 +303,23 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGraph g, Buffers b) {
   extern __shared__ int32_t s_acc[];  // WARPS x n_out
+  constexpr int kRowCap = 256;        // the node's own row, staged when it fits
+  __shared__ int32_t s_rows[WARPS][kRowCap];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int32_t* acc = s_acc + warp * m.n_out;
+  int32_t* srow = s_rows[warp];
   const int n_nodes = b.st->n_nodes;
   const uint32_t step = b.st->step;
   const Stream rs{m.seed, m.chain};
   const uint64_t cap = 64ull * (uint64_t)m.n_out + 4096ull;
   for (int slot = blockIdx.x * WARPS + warp; slot < n_nodes; slot += gridDim.x * WARPS) {
     const int32_t i = b.nodes[slot];
+    const int64_t ir0 = g.row_ptr[i];
+    const int32_t ideg = (int32_t)(g.row_ptr[i + 1] - ir0);
+    const bool row_in_smem = ideg <= kRowCap;
+    if (row_in_smem)
+      for (int q = lane; q < ideg; q += 32) srow[q] = g.col[ir0 + q];
+    __syncwarp();
     int count = 0;
     uint64_t t = 0;
     while (count < m.n_out) {
@@ -284,7 +328,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
         break;
       }
       const int32_t j = (int32_t)(rs.draw_u64(kTagNbr, (uint32_t)i, step, t + lane) % (uint64_t)g.n);
-      bool ok = (j != i) && !is_excluded(g, i, j);
+      const unsigned long long key = pair_key(i, j);
+      const unsigned long long xs = hash64(key) & g.excl_mask;
+      const unsigned long long xk = __ldg(g.excl + xs);
+      bool ok = (j != i) && !probe_resolve(g.excl, g.excl_mask, key, xs, xk);
       for (int q = 0; q < count && ok; ++q) ok = (acc[q] != j);
       const uint32_t peers = __match_any_sync(0xffffffffu, j);
       ok = ok && ((peers & lanemask_lt()) == 0);
@@ -294,14 +341,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
       if (ok && pos < need) {
         const int idx = count + pos;
         acc[idx] = j;
-        const uint32_t y = has_edge(g, i, j) ? 1u : 0u;
+        const uint32_t y = (row_in_smem ? row_contains(srow, ideg, j) : has_edge(g, i, j)) ? 1u : 0u;
         b.nbr[(int64_t)slot * m.n_out + idx] = (uint32_t)j | (y << 31);
       }
       count += min(__popc(bal), need);
       t += 32;
       __syncwarp();
     }
-    __syncwarp();
+    __syncwarp();  // srow and acc are reused by the warp's next node
   }
 }
 
@@ -546,6 +593,7 @@ __global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int nco
   __shared__ float s_part[4][2][KQ * 128];
   const int bb = blockIdx.x - ncommit;
   const int n_edges = b.st->n_edges;
+  if (bb * 4 >= n_edges) return;  // no edges for this block: k_theta skips its partial
   float R0[KQ * 4], R1[KQ * 4], bt[KQ * 4];
 #pragma unroll
   for (int q = 0; q < KQ; ++q)
@@ -617,45 +665,45 @@ __global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int nco
 //   G_k0 = beta R1 (0 - 1/ts) + (1-beta) R0 (1/theta_k0 - 1/ts)
 //   G_k1 = beta R1 (1/theta_k1 - 1/ts) + (1-beta) R0 (0 - 1/ts)
 // ---------------------------------------------------------------------------
-static __global__ void __launch_bounds__(256) k_theta(Model m, Buffers b) {
-  // 32 consecutive k per CTA; warp w sums block partials w, w+8, ... in FP64,
-  // then warp 0 adds the eight warp sums in fixed order (deterministic).
-  __shared__ double s_r0[8][32], s_r1[8][32];
+static __global__ void __launch_bounds__(1024) k_theta(Model m, Buffers b) {
+  // 32 consecutive k per CTA; warp w sums the partials of the active beta
+  // blocks w, w+32, ... in FP32 with Kahan compensation, then warp 0 adds
+  // the 32 warp sums in fixed order (deterministic) and takes the FP64 step.
+  __shared__ float s_r0[32][33], s_c0[32][33], s_r1[32][33], s_c1[32][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + lane;
   const int Kp = m.Kp;
-  double r0 = 0.0, r1 = 0.0;
+  const int active = min(m.nbb, (b.st->n_edges + 3) / 4);  // blocks that saw edges
+  float r0 = 0.f, c0 = 0.f, r1 = 0.f, c1 = 0.f;
   if (k < m.K) {
-    int bb = warp;
-    for (; bb + 24 < m.nbb; bb += 32) {
+    for (int bb = warp; bb < active; bb += 32) {
       const float* p0 = b.beta_part + (int64_t)bb * 2 * Kp + k;
-      const float a0 = p0[0], a1 = p0[8 * 2 * Kp], a2 = p0[16 * 2 * Kp], a3 = p0[24 * 2 * Kp];
-      const float c0 = p0[Kp], c1 = p0[8 * 2 * Kp + Kp], c2 = p0[16 * 2 * Kp + Kp],
-                  c3 = p0[24 * 2 * Kp + Kp];
-      r0 += (double)a0;
-      r0 += (double)a1;
-      r0 += (double)a2;
-      r0 += (double)a3;
-      r1 += (double)c0;
-      r1 += (double)c1;
-      r1 += (double)c2;
-      r1 += (double)c3;
-    }
-    for (; bb < m.nbb; bb += 8) {
-      r0 += (double)b.beta_part[(int64_t)bb * 2 * Kp + k];
-      r1 += (double)b.beta_part[(int64_t)bb * 2 * Kp + Kp + k];
+      const float y0 = p0[0] - c0, y1 = p0[Kp] - c1;
+      const float t0 = r0 + y0, t1 = r1 + y1;
+      c0 = (t0 - r0) - y0;
+      c1 = (t1 - r1) - y1;
+      r0 = t0;
+      r1 = t1;
     }
   }
   s_r0[warp][lane] = r0;
+  s_c0[warp][lane] = c0;
   s_r1[warp][lane] = r1;
+  s_c1[warp][lane] = c1;
   __syncthreads();
   if (warp != 0 || k >= m.K) return;
-  double R0 = 0.0, R1 = 0.0;
+  float a0 = 0.f, e0 = 0.f, a1 = 0.f, e1 = 0.f;  // Kahan over the 32 warp sums
 #pragma unroll
-  for (int w = 0; w < 8; ++w) {
-    R0 += s_r0[w][lane];
-    R1 += s_r1[w][lane];
+  for (int w = 0; w < 32; ++w) {
+    const float y0 = (s_r0[w][lane] - s_c0[w][lane]) - e0;
+    const float y1 = (s_r1[w][lane] - s_c1[w][lane]) - e1;
+    const float t0 = a0 + y0, t1 = a1 + y1;
+    e0 = (t0 - a0) - y0;
+    e1 = (t1 - a1) - y1;
+    a0 = t0;
+    a1 = t1;
   }
+  const double R0 = (double)a0 - (double)e0, R1 = (double)a1 - (double)e1;
   const uint32_t step = b.st->step;
   const double eps_t = (double)b.st->eps;
   const double scale = (double)b.st->scale;

@@ -76,6 +76,51 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
       : "memory");
 }
 
+// Packed FP32 pairs (Blackwell fma.rn.f32x2): two IEEE round-to-nearest
+// FMAs per instruction, element-wise identical to two scalar fmaf.
+typedef unsigned long long f32x2;
+
+__device__ __forceinline__ f32x2 pack_f32x2(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+
+__device__ __forceinline__ void unpack_f32x2(f32x2 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+__device__ __forceinline__ f32x2 fma_f32x2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// The 16 bytes of a row vector as EV/2 float pairs.
+template <typename PiT>
+struct PairLoad;
+
+template <>
+struct PairLoad<float> {
+  __device__ __forceinline__ static void get(const uint4& v, f32x2* out) {
+    out[0] = pack_f32x2(__uint_as_float(v.x), __uint_as_float(v.y));
+    out[1] = pack_f32x2(__uint_as_float(v.z), __uint_as_float(v.w));
+  }
+};
+
+template <>
+struct PairLoad<__nv_bfloat16> {
+  __device__ __forceinline__ static f32x2 word(uint32_t w) {
+    return pack_f32x2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+  }
+  __device__ __forceinline__ static void get(const uint4& v, f32x2* out) {
+    out[0] = word(v.x);
+    out[1] = word(v.y);
+    out[2] = word(v.z);
+    out[3] = word(v.w);
+  }
+};
+
 template <typename PiT, int VPL, int SPLIT, int STAGES>
 struct PhiTmaSmem {
   static size_t bytes(int Kp, int n_out) {
@@ -155,14 +200,17 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
 
     // ---- rows of this warp: q = warp + SPLIT * t
     const int T = (!dead && n_out > warp) ? (n_out - warp + SPLIT - 1) / SPLIT : 0;
-    float w[EPL], A[EPL];
+    constexpr int NP = EPL / 2;  // float pairs per lane
+    f32x2 w2[NP], A2[NP];
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
       const int vi = lane + 32 * v;
 #pragma unroll
-      for (int e = 0; e < EV; ++e) {
-        w[v * EV + e] = (vi < nvec) ? s_w[vi * EV + e] : 0.f;
-        A[v * EV + e] = 0.f;
+      for (int e = 0; e < EV; e += 2) {
+        const float lo = (vi < nvec) ? s_w[vi * EV + e] : 0.f;
+        const float hi = (vi < nvec) ? s_w[vi * EV + e + 1] : 0.f;
+        w2[(v * EV + e) / 2] = pack_f32x2(lo, hi);
+        A2[(v * EV + e) / 2] = pack_f32x2(0.f, 0.f);
       }
     }
     if (lane == 0) {
@@ -187,20 +235,28 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
         break;
       }
       const PiT* row = my_ring + (size_t)stg * Kp;
-      // the lane's slice of the row, unpacked once for both FMA passes
-      float x[EPL];
+      // the lane's slice of the row as float pairs, loaded once for both passes
+      f32x2 x2[NP];
 #pragma unroll
       for (int v = 0; v < VPL; ++v) {
         const int vi = lane + 32 * v;
         const uint4 raw = (vi < nvec) ? *reinterpret_cast<const uint4*>(row + vi * EV)
                                       : make_uint4(0, 0, 0, 0);
-        TR::unpack(raw, x + v * EV);
+        PairLoad<PiT>::get(raw, x2 + v * (EV / 2));
       }
-      // four independent partial sums break the FMA dependency chain
-      float d4[4] = {0.f, 0.f, 0.f, 0.f};
+      // four independent pair accumulators break the FMA dependency chain
+      f32x2 d2[4] = {0ull, 0ull, 0ull, 0ull};
 #pragma unroll
-      for (int e = 0; e < EPL; ++e) d4[e & 3] = fmaf(w[e], x[e], d4[e & 3]);
-      float D = (d4[0] + d4[1]) + (d4[2] + d4[3]);
+      for (int e = 0; e < NP; ++e) d2[e & 3] = fma_f32x2(w2[e], x2[e], d2[e & 3]);
+      float D;
+      {
+        float a0, a1, b0, b1, c0, c1, e0, e1;
+        unpack_f32x2(d2[0], a0, a1);
+        unpack_f32x2(d2[1], b0, b1);
+        unpack_f32x2(d2[2], c0, c1);
+        unpack_f32x2(d2[3], e0, e1);
+        D = ((a0 + a1) + (b0 + b1)) + ((c0 + c1) + (e0 + e1));
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) D += __shfl_xor_sync(0xffffffffu, D, o);
       const uint32_t word = s_nb[warp + SPLIT * t];
@@ -211,8 +267,9 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
       const float invP = __frcp_rn(P);
       const float cj = sgn * invP;
       Bsum += (ej * one_m_si - sgn * D) * invP;
+      const f32x2 c2 = pack_f32x2(cj, cj);
 #pragma unroll
-      for (int e = 0; e < EPL; ++e) A[e] = fmaf(cj, x[e], A[e]);
+      for (int e = 0; e < NP; ++e) A2[e] = fma_f32x2(c2, x2[e], A2[e]);
       __syncwarp();
       if (lane == 0 && t + STAGES < T) {  // refill this stage with row t + STAGES
         const uint32_t j = s_nb[warp + SPLIT * (t + STAGES)] & 0x7fffffffu;
@@ -241,7 +298,12 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
       const int vi = lane + 32 * v;
       if (vi < nvec) {
 #pragma unroll
-        for (int e = 0; e < EV; ++e) s_A[(size_t)warp * Kp + vi * EV + e] = A[v * EV + e];
+        for (int e = 0; e < EV; e += 2) {
+          float lo, hi;
+          unpack_f32x2(A2[(v * EV + e) / 2], lo, hi);
+          s_A[(size_t)warp * Kp + vi * EV + e] = lo;
+          s_A[(size_t)warp * Kp + vi * EV + e + 1] = hi;
+        }
       }
     }
     if (lane == 0) s_red[2 * SPLIT + warp] = Bsum;
