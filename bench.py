@@ -62,6 +62,7 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.path = None
+        self.skip = 0
 
     def start(self):
         try:
@@ -73,6 +74,19 @@ class ClockSampler:
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # nvidia-smi takes a moment to start: wait (at most 10 s) for its
+        # first sample so that the timed region is covered from its start
+        t0 = time.time()
+        while time.time() - t0 < 10.0 and self.proc.poll() is None:
+            if self._lines():
+                break
+            time.sleep(0.02)
+        self.skip = len(self._lines())
+
+    def _lines(self):
+        with open(self.path) as f:
+            return [ln for ln in f.read().splitlines() if ln.count(",") >= 8]
 
     def stop(self):
         if self.proc is None:
@@ -84,19 +98,19 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        with open(self.path) as f:
-            for line in f:
-                parts = [x.strip() for x in line.split(",")]
-                if len(parts) < 9:
-                    continue
-                try:
-                    sm.append(float(parts[1]))
-                    smax = float(parts[2])
-                except ValueError:
-                    continue
-                for n, v in zip(names, parts[5:9]):
-                    if v.lower() == "active":
-                        reasons.add(n)
+        lines = self._lines()
+        if len(lines) > self.skip:  # samples taken after the timed region began
+            lines = lines[self.skip:]
+        for line in lines:
+            parts = [x.strip() for x in line.split(",")]
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
         os.unlink(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
                 "reasons": sorted(reasons), "samples": len(sm)}
@@ -277,13 +291,18 @@ def ours_arm(args, net, opts, rank, world, local):
             nl_n += 1
     peaks, peak_src = load_peaks()
     achieved = phi_bytes / (phi_ms / 1000.0) / 1e9 if phi_ms > 0 else 0.0
+    # DRAM bytes per launch: the ncu-measured bytes per edge evaluation of
+    # the update_phi kernel (same K, n_out and pi type) times this run's
+    # mean evaluations per launch
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "update_phi_traffic.json")
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and args.profile_steps > 0:
         with open(tpath) as f:
             tr = json.load(f)
-        if tr.get("workload") == args.workload and tr.get("pi_dtype") == args.pi_dtype:
-            traffic = tr.get("bytes_per_launch")
+        if (tr.get("K") == K and tr.get("n_out") == n_out and tr.get("pi_dtype") == args.pi_dtype
+                and tr.get("bytes_per_eval")):
+            traffic = tr["bytes_per_eval"] * (phi_bytes / phi_bytes_per_eval(K, pi_bytes, n_out)) \
+                / args.profile_steps
 
     # e2e: the public run() loop (perplexity every interval, host reads)
     e2e = None
@@ -352,7 +371,7 @@ def ours_arm(args, net, opts, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large", choices=["large", "large_s", "mid", "small"])

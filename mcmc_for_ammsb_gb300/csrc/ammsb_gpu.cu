@@ -615,7 +615,8 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
 #undef TRY
   h->ncommit = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 3) / 4, 152 * 8));
   h->nbr_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 7) / 8, 152 * 8));
-  h->nbr_smem = (size_t)8 * m.n_out * sizeof(int32_t);
+  h->m.nbr_set_cap = next_pow2(std::max<int64_t>(64, 2 * (int64_t)m.n_out));
+  h->nbr_smem = (size_t)8 * h->m.nbr_set_cap * sizeof(int32_t);
   if (h->nbr_smem > 48 * 1024) {
     if (cudaFuncSetAttribute(k_sample_neighbors<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)h->nbr_smem) != cudaSuccess) {

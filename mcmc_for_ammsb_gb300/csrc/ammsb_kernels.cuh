@@ -33,6 +33,7 @@ struct Model {
   int32_t strategy;
   float nonlink_scale, link_scale;
   int32_t nbb;    // beta partial blocks
+  int32_t nbr_set_cap;  // per-warp accepted-neighbour set capacity (power of two)
 };
 
 struct Buffers {
@@ -72,6 +73,36 @@ __device__ __forceinline__ uint32_t group_mask(int lane) {
   } else {
     return ((1u << G) - 1u) << ((lane / G) * G);
   }
+}
+
+// Exclusive prefix sum of per-thread counts over a 1024-thread block, in
+// thread order; returns the position and sets *total.  Uses s_warp[33].
+__device__ __forceinline__ int block_scan_count_1024(int v, int* s_warp, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int n = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += n;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const int w = s_warp[lane];
+    int winc = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, winc, o);
+      if (lane >= o) winc += n;
+    }
+    s_warp[lane] = winc - w;
+    if (lane == 31) s_warp[32] = winc;
+  }
+  __syncthreads();
+  const int pos = s_warp[warp] + incl - v;
+  *total = s_warp[32];
+  __syncthreads();
+  return pos;
 }
 
 // Exclusive prefix count of `flag` over a 1024-thread block, in thread
@@ -125,10 +156,9 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
     const uint32_t step = b.gc->next_step;
     b.st->step = step;
     b.gc->next_step = step + 1;
-    b.st->eps = eps_schedule(m.a, m.b, m.c, step);
     int flag;
     if (m.strategy == 0)
-      flag = (int)(rs.draw_u64(kTagMbFlag, 0, step, 0) % 2ull);
+      flag = (int)uniform_below(rs.draw_u64(kTagMbFlag, 0, step, 0), 2ull);
     else
       flag = (m.strategy == 1) ? 1 : 0;
     s_flag = flag;
@@ -138,11 +168,14 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
   __syncthreads();
   const uint32_t step = s_step;
   const int flag = s_flag;
+  // eps_t is only read by the update kernels: one thread of warp 1 computes
+  // it (FP64 pow) off the sampling critical path
+  if (tid == 32) b.st->eps = eps_schedule(m.a, m.b, m.c, step);
   int err = 0;
   int rounds = 0;
   if (flag == 0) {
     const int mb = m.mini_batch_size;
-    const int32_t v = (int32_t)(rs.draw_u64(kTagMbNode, 0, step, 0) % (uint64_t)g.n);
+    const int32_t v = (int32_t)uniform_below(rs.draw_u64(kTagMbNode, 0, step, 0), (uint64_t)g.n);
     uint32_t* hkey = smem_hash ? s_htab : b.htab_key;
     uint32_t* hidx = smem_hash ? s_htab + (b.hmask + 1) : b.htab_idx;
     for (uint32_t s = tid; s <= b.hmask; s += blockDim.x) {
@@ -166,18 +199,21 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
         err |= kErrMinibatchCap;
         break;
       }
-      // pass A: validity and first-occurrence index per value; G candidates
-      // per thread with the first probes of both hashes issued together
+      // pass A: validity and first-occurrence index per value.  Thread tid
+      // owns the G consecutive candidates c0 + G*tid + j of each chunk of
+      // G*blockDim.x; the first exclusion probes of all G are issued together.
       constexpr int G = 4;
-      for (int c0 = tid; c0 < need; c0 += blockDim.x * G) {
+      const int chunk = G * (int)blockDim.x;
+      for (int c0 = 0; c0 < need; c0 += chunk) {
         int32_t u[G];
         bool live[G];
         unsigned long long key[G], xs[G], xk[G];
 #pragma unroll
         for (int j = 0; j < G; ++j) {
-          const int c = c0 + j * blockDim.x;
+          const int c = c0 + G * tid + j;
           live[j] = c < need;
-          u[j] = live[j] ? (int32_t)(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c) % (uint64_t)g.n)
+          u[j] = live[j] ? (int32_t)uniform_below(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c),
+                                                  (uint64_t)g.n)
                          : -1;
           live[j] = live[j] && (u[j] != v);
           key[j] = pair_key(v, u[j] < 0 ? 0 : u[j]);
@@ -187,7 +223,7 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
         for (int j = 0; j < G; ++j) xk[j] = live[j] ? __ldg(g.excl + xs[j]) : kEmptyKey;
 #pragma unroll
         for (int j = 0; j < G; ++j) {
-          const int c = c0 + j * blockDim.x;
+          const int c = c0 + G * tid + j;
           if (c >= need) continue;
           const bool linked = live[j] && (row_in_smem ? row_contains(s_row, vdeg, u[j])
                                                       : has_edge(g, v, u[j]));
@@ -208,34 +244,46 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
         }
       }
       __syncthreads();
-      // pass B: ordered compaction of first occurrences
-      for (int base = 0; base < need; base += blockDim.x) {
-        const int c = base + tid;
-        int32_t u = -1;
-        bool acc = false;
-        if (c < need) {
-          u = b.cand[c];
-          if (u >= 0) {
-            uint32_t slot = hash32((uint32_t)u) & b.hmask;
-            for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
-              const uint32_t k = hkey[slot];
-              if (k == (uint32_t)u) {
-                acc = (hidx[slot] == (uint32_t)(t + (uint64_t)c));
-                break;
+      // pass B: ordered compaction of first occurrences, one block scan per
+      // chunk (thread-local counts of G consecutive candidates)
+      for (int c0 = 0; c0 < need; c0 += chunk) {
+        int32_t u[G];
+        bool acc[G];
+        int mine = 0;
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+          const int c = c0 + G * tid + j;
+          u[j] = -1;
+          acc[j] = false;
+          if (c < need) {
+            u[j] = b.cand[c];
+            if (u[j] >= 0) {
+              uint32_t slot = hash32((uint32_t)u[j]) & b.hmask;
+              for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
+                const uint32_t kk = hkey[slot];
+                if (kk == (uint32_t)u[j]) {
+                  acc[j] = (hidx[slot] == (uint32_t)(t + (uint64_t)c));
+                  break;
+                }
+                if (kk == 0xffffffffu) break;
+                slot = (slot + 1) & b.hmask;
               }
-              if (k == 0xffffffffu) break;
-              slot = (slot + 1) & b.hmask;
             }
           }
+          mine += acc[j] ? 1 : 0;
         }
         int total;
-        const int pos = block_scan_1024(acc, s_warp, &total);
-        if (acc) {
-          const int e = count + pos;
-          b.nodes[e + 1] = u;
-          b.ea[e] = 0;
-          b.eb[e] = e + 1;
-          b.ey[e] = 0;
+        int pos = block_scan_count_1024(mine, s_warp, &total);
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+          if (acc[j]) {
+            const int e = count + pos;
+            b.nodes[e + 1] = u[j];
+            b.ea[e] = 0;
+            b.eb[e] = e + 1;
+            b.ey[e] = 0;
+            ++pos;
+          }
         }
         count += total;
       }
@@ -250,7 +298,8 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
   } else {
     int count = 0;
     for (int attempt = 0; attempt < 4096 && count == 0 && !err; ++attempt) {
-      const int32_t v = (int32_t)(rs.draw_u64(kTagMbNode, 0, step, (uint64_t)attempt) % (uint64_t)g.n);
+      const int32_t v =
+          (int32_t)uniform_below(rs.draw_u64(kTagMbNode, 0, step, (uint64_t)attempt), (uint64_t)g.n);
       const int64_t r0 = g.row_ptr[v], deg = g.row_ptr[v + 1] - r0;
       if (deg > m.max_edges || deg + 1 > m.max_nodes) {
         err |= kErrCapacity;
@@ -302,11 +351,14 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
 // ---------------------------------------------------------------------------
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGraph g, Buffers b) {
-  extern __shared__ int32_t s_acc[];  // WARPS x n_out
-  constexpr int kRowCap = 256;        // the node's own row, staged when it fits
+  // per warp: a set of the ids accepted so far (open addressing, capacity a
+  // power of two >= 2 n_out, -1 empty) in dynamic shared memory
+  extern __shared__ int32_t s_sets[];
+  constexpr int kRowCap = 256;  // the node's own row, staged when it fits
   __shared__ int32_t s_rows[WARPS][kRowCap];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int32_t* acc = s_acc + warp * m.n_out;
+  const uint32_t smask = (uint32_t)m.nbr_set_cap - 1u;
+  int32_t* set = s_sets + (size_t)warp * m.nbr_set_cap;
   int32_t* srow = s_rows[warp];
   const int n_nodes = b.st->n_nodes;
   const uint32_t step = b.st->step;
@@ -319,6 +371,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
     const bool row_in_smem = ideg <= kRowCap;
     if (row_in_smem)
       for (int q = lane; q < ideg; q += 32) srow[q] = g.col[ir0 + q];
+    for (uint32_t q = lane; q <= smask; q += 32) set[q] = -1;
     __syncwarp();
     int count = 0;
     uint64_t t = 0;
@@ -327,20 +380,37 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
         if (lane == 0) atomicOr(&b.gc->err, kErrNeighborCap);
         break;
       }
-      const int32_t j = (int32_t)(rs.draw_u64(kTagNbr, (uint32_t)i, step, t + lane) % (uint64_t)g.n);
+      const int32_t j = (int32_t)uniform_below(rs.draw_u64(kTagNbr, (uint32_t)i, step, t + lane),
+                                               (uint64_t)g.n);
       const unsigned long long key = pair_key(i, j);
       const unsigned long long xs = hash64(key) & g.excl_mask;
       const unsigned long long xk = __ldg(g.excl + xs);
       bool ok = (j != i) && !probe_resolve(g.excl, g.excl_mask, key, xs, xk);
-      for (int q = 0; q < count && ok; ++q) ok = (acc[q] != j);
+      if (ok) {  // already accepted in an earlier round?
+        uint32_t h = hash32((uint32_t)j) & smask;
+        for (uint32_t probe = 0; probe <= smask; ++probe) {
+          const int32_t e = set[h];
+          if (e == j) {
+            ok = false;
+            break;
+          }
+          if (e < 0) break;
+          h = (h + 1) & smask;
+        }
+      }
       const uint32_t peers = __match_any_sync(0xffffffffu, j);
       ok = ok && ((peers & lanemask_lt()) == 0);
       const uint32_t bal = __ballot_sync(0xffffffffu, ok);
       const int pos = __popc(bal & lanemask_lt());
       const int need = m.n_out - count;
+      __syncwarp();  // every lane has probed the set before it grows
       if (ok && pos < need) {
         const int idx = count + pos;
-        acc[idx] = j;
+        uint32_t h = hash32((uint32_t)j) & smask;
+        for (uint32_t probe = 0; probe <= smask; ++probe) {
+          if (atomicCAS(set + h, -1, j) == -1) break;
+          h = (h + 1) & smask;
+        }
         const uint32_t y = (row_in_smem ? row_contains(srow, ideg, j) : has_edge(g, i, j)) ? 1u : 0u;
         b.nbr[(int64_t)slot * m.n_out + idx] = (uint32_t)j | (y << 31);
       }
@@ -348,7 +418,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
       t += 32;
       __syncwarp();
     }
-    __syncwarp();  // srow and acc are reused by the warp's next node
+    __syncwarp();  // srow and set are reused by the warp's next node
   }
 }
 

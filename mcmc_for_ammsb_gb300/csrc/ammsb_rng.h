@@ -8,9 +8,9 @@
 //   counter = {block index, entity, step, tag | (block index >> 32) << 8}
 //   key     = {seed, chain}
 // and the derived draws used by the hot path:
-//   * draw_u64(t): 64 bits from half t%2 of block t/2; uniform integers are
-//     draw_u64 % range, the reference's randint() = rand() % range rule
-//     (random.cc:174-176) on a 64-bit source;
+//   * draw_u64(t): 64 bits from half t%2 of block t/2; uniform integers in
+//     [0, range) are uniform_below(draw, range) = floor(draw * range / 2^64)
+//     (the reference's randint() reduces rand() % range, random.cc:174-176);
 //   * normal(idx): Box-Muller on 24-bit uniforms, 4 normals per block.
 // The same code compiles for the host (graph generator, theta init) and the
 // device (sampling kernels), so integer draws agree bit for bit.
@@ -91,6 +91,17 @@ struct Stream {
                    : ((uint64_t)o.x | ((uint64_t)o.y << 32));
   }
 };
+
+// Uniform integer in [0, n): floor(x * n / 2^64), the multiply-high map of a
+// 64-bit draw (bias at most n / 2^64).  A 64-bit remainder would run through
+// the slow FP64 path of the GPU.
+AMMSB_HD uint64_t uniform_below(uint64_t x, uint64_t n) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(x, n);
+#else
+  return (uint64_t)(((unsigned __int128)x * (unsigned __int128)n) >> 64);
+#endif
+}
 
 // 24-bit uniforms are exact in float everywhere.
 AMMSB_HD float u24_open(uint32_t x) {  // (0, 1)

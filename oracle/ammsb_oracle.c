@@ -66,6 +66,13 @@ uint64_t oracle_draw_u64(uint32_t seed, uint32_t chain, uint32_t tag,
   return (uint64_t)o[0] | ((uint64_t)o[1] << 32);
 }
 
+/* Uniform integer in [0, n) from a 64-bit draw: floor(x * n / 2^64). */
+static inline uint64_t below(uint64_t x, uint64_t n) {
+  return (uint64_t)(((unsigned __int128)x * (unsigned __int128)n) >> 64);
+}
+
+uint64_t oracle_uniform_below(uint64_t x, uint64_t n) { return below(x, n); }
+
 float oracle_normal(uint32_t seed, uint32_t chain, uint32_t tag,
                     uint32_t entity, uint32_t step, uint64_t idx) {
   uint32_t o[4];
@@ -186,8 +193,8 @@ static int sample_nonlinks(const oracle_graph *g, int64_t m, uint32_t seed,
                            oracle_mb_info *info) {
   int64_t N = g->n;
   if (m > max_edges || m + 1 > max_nodes) return -2;
-  int32_t v = (int32_t)(oracle_draw_u64(seed, chain, OR_P_MB_NODE, 0, step, 0) %
-                        (uint64_t)N);
+  int32_t v = (int32_t)below(oracle_draw_u64(seed, chain, OR_P_MB_NODE, 0, step, 0),
+                              (uint64_t)N);
   nodes[0] = v;
   int32_t count = 0;
   int64_t t = 0;
@@ -196,9 +203,9 @@ static int sample_nonlinks(const oracle_graph *g, int64_t m, uint32_t seed,
     int64_t need = m - count;
     if (t + need > NONLINK_CAND_CAP(m)) return -1;
     for (int64_t c = 0; c < need; ++c) {
-      int32_t u = (int32_t)(oracle_draw_u64(seed, chain, OR_P_MB_CAND, 0, step,
-                                            (uint64_t)(t + c)) %
-                            (uint64_t)N);
+      int32_t u = (int32_t)below(oracle_draw_u64(seed, chain, OR_P_MB_CAND, 0, step,
+                                                 (uint64_t)(t + c)),
+                                 (uint64_t)N);
       if (u == v) continue;
       if (oracle_has_edge(g, v, u) || oracle_is_excluded(g, v, u)) continue;
       if (in_list(nodes + 1, count, u)) continue;
@@ -226,9 +233,9 @@ static int sample_links(const oracle_graph *g, uint32_t seed, uint32_t chain,
                         oracle_mb_info *info) {
   int64_t N = g->n;
   for (int32_t attempt = 0; attempt < LINK_ATTEMPT_CAP; ++attempt) {
-    int32_t v = (int32_t)(oracle_draw_u64(seed, chain, OR_P_MB_NODE, 0, step,
-                                          (uint64_t)attempt) %
-                          (uint64_t)N);
+    int32_t v = (int32_t)below(oracle_draw_u64(seed, chain, OR_P_MB_NODE, 0, step,
+                                               (uint64_t)attempt),
+                               (uint64_t)N);
     int32_t count = 0;
     for (int64_t p = g->row_ptr[v]; p < g->row_ptr[v + 1]; ++p) {
       int32_t u = g->col[p];
@@ -260,7 +267,7 @@ int oracle_sample_minibatch(const oracle_graph *g, int strategy,
   int flag;
   if (strategy == 0) {
     /* network.cc:410-421: flag = randint(0, 1) */
-    flag = (int)(oracle_draw_u64(seed, chain, OR_P_MB_FLAG, 0, step, 0) % 2u);
+    flag = (int)below(oracle_draw_u64(seed, chain, OR_P_MB_FLAG, 0, step, 0), 2u);
   } else if (strategy == 1) {
     flag = 1;
   } else if (strategy == 2) {
@@ -289,9 +296,9 @@ int64_t oracle_sample_neighbors(const oracle_graph *g, int32_t node,
   int64_t t = 0;
   while (count < n_out) {
     if (t >= cap) return -1;
-    int32_t j = (int32_t)(oracle_draw_u64(seed, chain, OR_P_NBR,
-                                          (uint32_t)node, step, (uint64_t)t) %
-                          (uint64_t)g->n);
+    int32_t j = (int32_t)below(oracle_draw_u64(seed, chain, OR_P_NBR, (uint32_t)node, step,
+                                               (uint64_t)t),
+                               (uint64_t)g->n);
     t++;
     if (j == node) continue;
     if (oracle_is_excluded(g, node, j)) continue;

@@ -48,6 +48,10 @@ enum {
 uint64_t oracle_draw_u64(uint32_t seed, uint32_t chain, uint32_t tag,
                          uint32_t entity, uint32_t step, uint64_t t);
 
+/* Uniform integer in [0, n) from a 64-bit draw x: floor(x * n / 2^64) (the
+ * multiply-high map; the reference reduces rand() % range, random.cc:174). */
+uint64_t oracle_uniform_below(uint64_t x, uint64_t n);
+
 /* Standard normals of stream (tag, entity, step), element idx: Box-Muller on
  * 24-bit uniforms, four normals per Philox block. */
 float oracle_normal(uint32_t seed, uint32_t chain, uint32_t tag,
