@@ -46,6 +46,10 @@ extern "C" {
 #define AMMSB_PI_F32 0
 #define AMMSB_PI_BF16 1
 
+/* Element types of the edge log-likelihood and its adjoint. */
+#define AMMSB_REAL_F32 0
+#define AMMSB_REAL_F64 1
+
 /* The sampler's option surface, options.h:142-185 (mcmc.* flags).  Zero
  * values take the reference's derived defaults at ammsb_create():
  * a := b^-c (options.h:257-259), alpha := 1/K (options.h:260-262),
@@ -188,6 +192,19 @@ void *ammsb_stream(ammsb_handle *h);
 int ammsb_get_counters(ammsb_handle *h, uint64_t *edge_evals,
                        uint64_t *iterations);
 
+/* Checkpoint and resume.  No counterpart in the reference's sequential
+ * sampler (its state lives only in memory).  ammsb_save_checkpoint writes
+ * the whole chain to `path`: phi, the stored pi bit for bit (F32 or BF16),
+ * theta, beta, the held-out running averages, step_count, average_count, the
+ * perplexity history of the convergence test (learner.cc:130-136) and the
+ * Philox key (seed, chain).  Every draw is a function of (seed, chain,
+ * step), so a handle created with the same options and data that loads the
+ * checkpoint continues the trajectory bit for bit.  ammsb_load_checkpoint
+ * rejects (AMMSB_E_ARG) a file whose pi type, N, K, held-out set, seed or
+ * chain differ from the handle's.  Both synchronise the handle's stream. */
+int ammsb_save_checkpoint(ammsb_handle *h, const char *path);
+int ammsb_load_checkpoint(ammsb_handle *h, const char *path);
+
 /* Held-out perplexity without any device allocation.  No counterpart in
  * the reference: it serves callers that cannot call cudaMalloc (a host
  * program whose runtime owns every device allocation, or that must not
@@ -210,6 +227,62 @@ int ammsb_perplexity_noalloc(const void *pi, int32_t pi_dtype, int64_t K,
                              int64_t held_count, float *ppx,
                              uint64_t average_count, void *stream,
                              double *out);
+
+/* ------------------------------------------------------------------------ */
+/* Minibatch edge log-likelihood and its adjoint (the SGRLD drift).        */
+/* ------------------------------------------------------------------------ */
+/* L = sum over pairs q = (a, b, y) of log p_q, with
+ *   p_q = sum_k pi_ak pi_bk (f_qk - e_q) + e_q,  pi_a = phi_a / sum(phi_a),
+ *   f = y ? beta : 1 - beta,  e = y ? epsilon : 1 - epsilon,
+ *   beta_k = theta_k1 / (theta_k0 + theta_k1):
+ * the probability update_beta normalises by (prob_sum,
+ * mcmc_sampler_stochastic.cc:212-240) of a source row given as phi and a
+ * neighbour row given as pi (cal_edge_likelihood, learner.h:100-139, leaves
+ * out eps * (1 - sum_k pi_ak pi_bk) for a link).  Its gradient in phi is the
+ * update_phi gradient
+ * (mcmc_sampler_stochastic.cc:274-296, neighbour pi held fixed) and in theta
+ * the update_beta gradient (cc:212-240): the hand-derived terms the
+ * reference uses as its SGRLD drift.  All arrays are device memory of
+ * element type dtype: phi_src n_src rows (stride ld_phi), pi_nbr n_nbr rows
+ * (stride ld_pi), theta K x 2.  Pairs are grouped by source: the pairs of
+ * source a are q in [src_ptr[a], src_ptr[a+1]), with neighbour row
+ * pair_nbr[q] and label pair_y[q].  The forward writes *loss (device) and
+ * keeps p_q and the row sums in `workspace` (caller-owned device memory of
+ * ammsb_edge_loglik_workspace_size bytes); the backward reads them back, so
+ * the two calls share one workspace and the same inputs.  Index errors in
+ * the pair arrays skip the pair and set bit 1 of the workspace's status
+ * word, a non-positive row sum or probability sets bit 2 (read with
+ * ammsb_edge_loglik_status).  Deterministic: every sum runs in a fixed
+ * order.  Kernels are queued on `stream`; nothing is synchronised. */
+size_t ammsb_edge_loglik_workspace_size(int32_t dtype, int64_t K,
+                                        int64_t n_src, int64_t n_pairs);
+int ammsb_edge_loglik_forward(int32_t dtype, int64_t K, const void *phi_src,
+                              int64_t ld_phi, const void *pi_nbr,
+                              int64_t ld_pi, int64_t n_nbr, const void *theta,
+                              double epsilon, const int64_t *src_ptr,
+                              int64_t n_src, const int32_t *pair_nbr,
+                              const uint8_t *pair_y, int64_t n_pairs,
+                              void *loss, void *workspace, void *stream);
+/* grad_loss: device scalar dL.  Writes grad_phi_src (n_src rows, stride
+ * ld_phi), grad_theta (K x 2) and, when grad_pi_nbr is not null, grad_pi_nbr
+ * (n_nbr rows, stride ld_pi), which needs the pairs grouped by neighbour
+ * too: the pairs of neighbour row b are nbr_pairs[r], r in
+ * [nbr_ptr[b], nbr_ptr[b+1]), and pair_src[q] is the source of pair q. */
+int ammsb_edge_loglik_backward(int32_t dtype, int64_t K, const void *phi_src,
+                               int64_t ld_phi, const void *pi_nbr,
+                               int64_t ld_pi, int64_t n_nbr,
+                               const void *theta, double epsilon,
+                               const int64_t *src_ptr, int64_t n_src,
+                               const int32_t *pair_nbr, const uint8_t *pair_y,
+                               int64_t n_pairs, const int32_t *pair_src,
+                               const int64_t *nbr_ptr,
+                               const int32_t *nbr_pairs, const void *grad_loss,
+                               void *grad_phi_src, void *grad_pi_nbr,
+                               void *grad_theta, void *workspace,
+                               void *stream);
+/* Status word of a workspace (bits above); synchronises `stream`. */
+int ammsb_edge_loglik_status(const void *workspace, void *stream,
+                             int32_t *flags);
 
 /* ------------------------------------------------------------------------ */
 /* Host-side data preparation (no GPU use).                                 */

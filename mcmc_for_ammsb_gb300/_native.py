@@ -27,6 +27,9 @@ RANDOM_EDGE = 3
 PI_F32 = 0
 PI_BF16 = 1
 
+REAL_F32 = 0
+REAL_F64 = 1
+
 
 class AmmsbOptions(ctypes.Structure):
     _fields_ = [
@@ -128,9 +131,21 @@ SIGNATURES = [
     ("ammsb_profile_step", ctypes.c_int, [_P, _F64P]),
     ("ammsb_stream", _P, [_P]),
     ("ammsb_get_counters", ctypes.c_int, [_P, _U64P, _U64P]),
+    ("ammsb_save_checkpoint", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("ammsb_load_checkpoint", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("ammsb_perplexity_noalloc", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
                                                 _P, ctypes.c_double, _P, _P, _P, ctypes.c_int64,
                                                 _P, ctypes.c_uint64, _P, _F64P]),
+    ("ammsb_edge_loglik_workspace_size", ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int64,
+                                                          ctypes.c_int64, ctypes.c_int64]),
+    ("ammsb_edge_loglik_forward", ctypes.c_int,
+     [ctypes.c_int32, ctypes.c_int64, _P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_int64, _P,
+      ctypes.c_double, _P, ctypes.c_int64, _P, _P, ctypes.c_int64, _P, _P, _P]),
+    ("ammsb_edge_loglik_backward", ctypes.c_int,
+     [ctypes.c_int32, ctypes.c_int64, _P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_int64, _P,
+      ctypes.c_double, _P, ctypes.c_int64, _P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P,
+      _P]),
+    ("ammsb_edge_loglik_status", ctypes.c_int, [_P, _P, _I32P]),
     ("ammsb_generate_graph", ctypes.c_int, [ctypes.POINTER(AmmsbGenParams), ctypes.POINTER(_P)]),
     ("ammsb_graph_from_edges", ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _I32P, _I32P,
                                               ctypes.POINTER(_P)]),

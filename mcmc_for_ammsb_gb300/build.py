@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libammsb_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-Wall", "-diag-suppress", "177"]
-SOURCES = ["ammsb_gpu.cu", "ammsb_host.cpp", "ammsb_noalloc.cu"]
+SOURCES = ["ammsb_gpu.cu", "ammsb_host.cpp", "ammsb_noalloc.cu", "ammsb_adjoint.cu"]
 
 
 def _nvcc():
@@ -44,7 +44,7 @@ def _deps():
 def build(force=False, verbose=False):
     """Compile libammsb_gpu.so if any source is newer; returns its path."""
     deps = _deps()
-    if not force and _newer(LIB, deps):
+    if not force and _newer(LIB, deps) and _newer(CLI, deps):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = _nvcc()
@@ -67,7 +67,25 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
+
+
+CLI = os.path.join(HERE, "ammsb_main")
+
+
+def build_cli():
+    """The command-line driver (csrc/ammsb_main.cpp), host C++ linked
+    against libammsb_gpu.so (found next to it at run time)."""
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(os.path.dirname(HERE), "include"),
+           os.path.join(CSRC, "ammsb_main.cpp"), "-L", HERE, "-lammsb_gpu",
+           "-Wl,-rpath,$ORIGIN", "-o", CLI + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":

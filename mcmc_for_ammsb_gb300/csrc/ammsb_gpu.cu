@@ -1059,4 +1059,191 @@ int ammsb_get_counters(ammsb_handle* h, uint64_t* edge_evals, uint64_t* iteratio
   return AMMSB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Checkpoint / resume.  Every draw is a function of (seed, chain, step), so
+// the state below is the whole chain: restoring it continues the trajectory
+// bit for bit.  Large arrays move through a bounded host staging buffer.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr char kCkMagic[8] = {'A', 'M', 'M', 'S', 'B', 'C', 'K', '1'};
+
+struct CkHeader {
+  int32_t pi_dtype, pad;
+  int64_t N, K, H;
+  uint32_t seed, chain;
+  uint64_t step_count, average_count, n_hist, held_sum;
+};
+
+uint64_t held_checksum(ammsb_handle* h) {
+  // FNV-1a over the held-out pairs (host copy of device arrays)
+  std::vector<int32_t> a(h->H), b(h->H);
+  std::vector<uint8_t> y(h->H);
+  if (h->H > 0) {
+    cudaMemcpy(a.data(), h->d_ha, sizeof(int32_t) * h->H, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b.data(), h->d_hb, sizeof(int32_t) * h->H, cudaMemcpyDeviceToHost);
+    cudaMemcpy(y.data(), h->d_hy, h->H, cudaMemcpyDeviceToHost);
+  }
+  uint64_t x = 1469598103934665603ull;
+  auto mix = [&](const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) x = (x ^ c[i]) * 1099511628211ull;
+  };
+  mix(a.data(), a.size() * 4);
+  mix(b.data(), b.size() * 4);
+  mix(y.data(), y.size());
+  return x;
+}
+
+// rows [0, N) of a device array with row stride Kp elements of es bytes,
+// K elements per row in the file
+int ck_rows(ammsb_handle* h, std::FILE* f, void* dev, size_t es, bool save) {
+  const int64_t N = h->m.N, K = h->m.K, Kp = h->m.Kp;
+  const int64_t rows_per = std::max<int64_t>(1, (64ll << 20) / (int64_t)(K * es));
+  std::vector<unsigned char> buf((size_t)std::min<int64_t>(rows_per, N) * (size_t)(K * es));
+  for (int64_t r0 = 0; r0 < N; r0 += rows_per) {
+    const int64_t n = std::min<int64_t>(rows_per, N - r0);
+    char* d = static_cast<char*>(dev) + (size_t)r0 * (size_t)Kp * es;
+    const size_t bytes = (size_t)n * (size_t)K * es;
+    if (save) {
+      CK(cudaMemcpy2DAsync(buf.data(), K * es, d, Kp * es, K * es, n, cudaMemcpyDeviceToHost,
+                           h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      if (std::fwrite(buf.data(), 1, bytes, f) != bytes) {
+        h->err = "checkpoint: write failed";
+        return AMMSB_E_ARG;
+      }
+    } else {
+      if (std::fread(buf.data(), 1, bytes, f) != bytes) {
+        h->err = "checkpoint: file is truncated";
+        return AMMSB_E_ARG;
+      }
+      CK(cudaMemcpy2DAsync(d, Kp * es, buf.data(), K * es, K * es, n, cudaMemcpyHostToDevice,
+                           h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+    }
+  }
+  return AMMSB_OK;
+}
+
+}  // namespace
+
+int ammsb_save_checkpoint(ammsb_handle* h, const char* path) {
+  if (!h || !path) return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    h->err = "no state to save: call ammsb_init_state or ammsb_set_state first";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  std::FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    h->err = std::string("checkpoint: cannot open ") + path;
+    return AMMSB_E_ARG;
+  }
+  CkHeader hd{};
+  hd.pi_dtype = h->opt.pi_dtype;
+  hd.N = h->m.N;
+  hd.K = h->m.K;
+  hd.H = h->H;
+  hd.seed = h->m.seed;
+  hd.chain = h->m.chain;
+  hd.step_count = h->step_count;
+  hd.average_count = h->average_count;
+  hd.n_hist = h->ppx_history.size();
+  hd.held_sum = held_checksum(h);
+  const int K = h->m.K;
+  std::vector<double> theta(2 * (size_t)K);
+  std::vector<float> beta(K), ppx(std::max<int64_t>(h->H, 1));
+  int rc = AMMSB_OK;
+  auto fail = [&](int code) {
+    std::fclose(f);
+    return code;
+  };
+  if (cudaMemcpy(theta.data(), h->b.theta, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost) ||
+      cudaMemcpy(beta.data(), h->b.beta, sizeof(float) * K, cudaMemcpyDeviceToHost) ||
+      (h->H > 0 && cudaMemcpy(ppx.data(), h->d_ppx, sizeof(float) * h->H, cudaMemcpyDeviceToHost))) {
+    h->err = "checkpoint: device read failed";
+    return fail(AMMSB_E_CUDA);
+  }
+  bool ok = std::fwrite(kCkMagic, 1, 8, f) == 8 && std::fwrite(&hd, sizeof(hd), 1, f) == 1 &&
+            std::fwrite(h->ppx_history.data(), sizeof(double), hd.n_hist, f) == hd.n_hist &&
+            std::fwrite(theta.data(), sizeof(double), theta.size(), f) == theta.size() &&
+            std::fwrite(beta.data(), sizeof(float), beta.size(), f) == beta.size() &&
+            std::fwrite(ppx.data(), sizeof(float), (size_t)h->H, f) == (size_t)h->H;
+  if (!ok) {
+    h->err = "checkpoint: write failed";
+    return fail(AMMSB_E_ARG);
+  }
+  if ((rc = ck_rows(h, f, h->b.phi, sizeof(float), true))) return fail(rc);
+  if ((rc = ck_rows(h, f, h->b.pi, (size_t)h->pi_bytes, true))) return fail(rc);
+  if (std::fclose(f) != 0) {
+    h->err = "checkpoint: close failed";
+    return AMMSB_E_ARG;
+  }
+  return AMMSB_OK;
+}
+
+int ammsb_load_checkpoint(ammsb_handle* h, const char* path) {
+  if (!h || !path) return AMMSB_E_ARG;
+  CK(cudaSetDevice(h->device));
+  std::FILE* f = std::fopen(path, "rb");
+  if (!f) {
+    h->err = std::string("checkpoint: cannot open ") + path;
+    return AMMSB_E_ARG;
+  }
+  auto fail = [&](const char* msg, int code) {
+    if (msg) h->err = msg;
+    std::fclose(f);
+    return code;
+  };
+  char magic[8];
+  CkHeader hd{};
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kCkMagic, 8) != 0 ||
+      std::fread(&hd, sizeof(hd), 1, f) != 1)
+    return fail("checkpoint: not a sampler checkpoint", AMMSB_E_ARG);
+  if (hd.pi_dtype != h->opt.pi_dtype || hd.N != h->m.N || hd.K != h->m.K || hd.H != h->H)
+    return fail("checkpoint: pi type, N, K or held-out size differ from this sampler", AMMSB_E_ARG);
+  if (hd.seed != h->m.seed || hd.chain != h->m.chain)
+    return fail("checkpoint: seed or chain differ from this sampler", AMMSB_E_ARG);
+  if (hd.held_sum != held_checksum(h))
+    return fail("checkpoint: held-out set differs from this sampler", AMMSB_E_ARG);
+  if (hd.step_count < 1 || hd.step_count > 0xffffffffull || hd.average_count < 1 ||
+      hd.n_hist > (1ull << 32))
+    return fail("checkpoint: corrupt counters", AMMSB_E_ARG);
+  const int K = h->m.K;
+  std::vector<double> hist(hd.n_hist), theta(2 * (size_t)K);
+  std::vector<float> beta(h->m.Kp, 0.f), ppx(std::max<int64_t>(h->H, 1));
+  if (std::fread(hist.data(), sizeof(double), hd.n_hist, f) != hd.n_hist ||
+      std::fread(theta.data(), sizeof(double), theta.size(), f) != theta.size() ||
+      std::fread(beta.data(), sizeof(float), K, f) != (size_t)K ||
+      std::fread(ppx.data(), sizeof(float), (size_t)h->H, f) != (size_t)h->H)
+    return fail("checkpoint: file is truncated", AMMSB_E_ARG);
+  if (cudaMemcpyAsync(h->b.theta, theta.data(), sizeof(double) * 2 * K, cudaMemcpyHostToDevice,
+                      h->stream) ||
+      cudaMemcpyAsync(h->b.beta, beta.data(), sizeof(float) * h->m.Kp, cudaMemcpyHostToDevice,
+                      h->stream) ||
+      (h->H > 0 && cudaMemcpyAsync(h->d_ppx, ppx.data(), sizeof(float) * h->H,
+                                   cudaMemcpyHostToDevice, h->stream)) ||
+      cudaStreamSynchronize(h->stream))
+    return fail("checkpoint: device write failed", AMMSB_E_CUDA);
+  int rc = ck_rows(h, f, h->b.phi, sizeof(float), false);
+  if (!rc) rc = ck_rows(h, f, h->b.pi, (size_t)h->pi_bytes, false);
+  if (rc) return fail(nullptr, rc);
+  std::fclose(f);
+  rc = reset_counters(h);  // zeroes the running averages: restore them after
+  if (rc) return rc;
+  if (h->H > 0)
+    CK(cudaMemcpyAsync(h->d_ppx, ppx.data(), sizeof(float) * h->H, cudaMemcpyHostToDevice,
+                       h->stream));
+  h->step_count = hd.step_count;
+  h->average_count = hd.average_count;
+  h->ppx_history = hist;
+  const uint32_t s = (uint32_t)hd.step_count;
+  CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->state_ready = true;
+  return AMMSB_OK;
+}
+
 }  // extern "C"

@@ -19,9 +19,12 @@
 
 #if defined(__CUDACC__)
 #define AMMSB_HD __host__ __device__ __forceinline__
-#define AMMSB_UNROLL _Pragma("unroll")
 #else
 #define AMMSB_HD inline
+#endif
+#ifdef __CUDA_ARCH__
+#define AMMSB_UNROLL _Pragma("unroll")
+#else
 #define AMMSB_UNROLL
 #endif
 

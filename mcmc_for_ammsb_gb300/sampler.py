@@ -80,9 +80,23 @@ class MCMCSamplerStochastic:
             self._h, phi.ctypes.data_as(_native._F32P), theta.ctypes.data_as(_native._F64P)))
         return self
 
+    def save_checkpoint(self, path):
+        """Writes the whole chain (state, counters, running averages, Philox
+        key) to `path`; see ammsb_save_checkpoint."""
+        self._check(_native.lib().ammsb_save_checkpoint(self._h, str(path).encode()))
+
+    def load_checkpoint(self, path):
+        """Restores a chain saved by save_checkpoint; the trajectory then
+        continues bit for bit."""
+        self.create()
+        self._check(_native.lib().ammsb_load_checkpoint(self._h, str(path).encode()))
+        return self
+
     # -- iteration ------------------------------------------------------------
     def run(self):
-        """MCMCSamplerStochastic::run (cc:93-183); returns the last perplexity."""
+        """MCMCSamplerStochastic::run (cc:93-183); returns the last perplexity.
+        Initialises the state first (init()) when nothing set it."""
+        self.create()
         out = ctypes.c_double()
         self._check(_native.lib().ammsb_run(self._h, ctypes.byref(out)))
         return out.value

@@ -214,6 +214,16 @@ def update_beta(K, pi, ea, eb, ey, theta, beta, eta, epsilon, eps, scale, noise,
     return th, bt, grads
 
 
+def edge_likelihood(K, pa, pb, y, beta, epsilon, dtype=np.float64):
+    """cal_edge_likelihood (learner.h:100-139) of one pair of pi rows."""
+    f64 = dtype == np.float64
+    real = ctypes.c_double if f64 else ctypes.c_float
+    fn = lib().oracle_edge_likelihood_f64 if f64 else lib().oracle_edge_likelihood_f32
+    return fn(ctypes.c_int32(K), _p(np.ascontiguousarray(pa, dtype)),
+              _p(np.ascontiguousarray(pb, dtype)), ctypes.c_int(int(y)),
+              _p(np.ascontiguousarray(beta, dtype)), real(epsilon))
+
+
 def normalize(phi, dtype=np.float32):
     phi = np.ascontiguousarray(phi, dtype)
     K = phi.shape[-1]

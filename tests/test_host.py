@@ -136,3 +136,71 @@ def test_create_without_gpu_fails_cleanly(native_lib):
     with pytest.raises(_native.AmmsbError) as e:
         MCMCSamplerStochastic(Options(K=8, num_node_sample=8), net).create()
     assert e.value.code == -2
+
+
+def test_edge_loglik_has_no_cpu_path(native_lib):
+    """The differentiable edge log-likelihood runs on the GPU only: CPU
+    tensors are refused before any kernel is queued, and the C ABI checks its
+    arguments before touching a device pointer."""
+    torch = pytest.importorskip("torch")
+    from mcmc_for_ammsb_gb300.autograd import edge_log_likelihood
+    x = torch.full((2, 4), 0.25, dtype=torch.float64)
+    th = torch.ones(4, 2, dtype=torch.float64)
+    idx = torch.zeros(3, dtype=torch.int64)
+    with pytest.raises(RuntimeError):
+        edge_log_likelihood(x, x, th, idx, idx, idx.to(torch.uint8), 1e-7)
+    L = native_lib
+    assert L.ammsb_edge_loglik_workspace_size(_native.REAL_F64, 16, 50, 1600) >= 8 * (
+        2 * 50 + 1600 + 50 * 16)
+    p = ctypes.c_void_p(256)
+    # unknown dtype, K out of range, stride below K: rejected without a GPU
+    for args in ((7, 16, 16), (_native.REAL_F64, 0, 16), (_native.REAL_F64, 2000, 2000),
+                 (_native.REAL_F64, 16, 8)):
+        dt, K, ld = args
+        assert L.ammsb_edge_loglik_forward(dt, K, p, ld, p, ld, 1, p, 1e-7, p, 1, p, p, 1, p, p,
+                                           None) == -1
+
+
+def _cli(args, **kw):
+    import subprocess
+    from mcmc_for_ammsb_gb300 import build
+    exe = build.CLI
+    return subprocess.run([exe] + list(args), capture_output=True, text=True, timeout=120, **kw)
+
+
+def test_cli_options_and_errors(native_lib, tmp_path):
+    """The C++ driver mirrors apps/main/main.cc: command-line echo, --help,
+    exit status 33 for option and IO errors (main.cc:79-86)."""
+    r = _cli(["--help"])
+    assert r.returncode == 0 and r.stdout.startswith("Command line: ")
+    for name in ("--mcmc.K [-K]", "--mcmc.mini-batch-size [-m]", "--mcmc.held-out-ratio [-h]",
+                 "--mcmc.strategy", "--mcmc.input.file [-f]", "--config"):
+        assert name in r.stdout
+    r = _cli(["--mcmc.strategy", "bogus"])
+    assert r.returncode == 33 and "Option error: Unknown strategy" in r.stderr
+    r = _cli(["-K", "12q"])
+    assert r.returncode == 33 and "Unknown characters in number" in r.stderr
+    r = _cli(["-K", "16", "--mcmc.K", "32"])
+    assert r.returncode == 33 and "more than once" in r.stderr
+    r = _cli(["-f", str(tmp_path / "missing.txt")])
+    assert r.returncode == 33 and "IO error" in r.stderr
+    cfg = tmp_path / "run.cfg"
+    cfg.write_text("[mcmc]\nK = 0x10\nbogus = 1\n")
+    r = _cli(["--config", str(cfg), "-c", "synthetic", "-f", "n=200,k_true=4"])
+    assert r.returncode == 33 and "unrecognised option 'mcmc.bogus'" in r.stderr
+
+
+def test_cli_reads_relativity_and_needs_a_gpu(native_lib, tmp_path):
+    """Without a GPU the driver gets as far as ammsb_create and reports the
+    CUDA error (no CPU fallback)."""
+    pytest.importorskip("torch")
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    net = Network.synthetic(n=300, k_true=6, size_min=10, size_max=100, intra_degree=4.0, seed=1)
+    path = tmp_path / "g.txt"
+    net.write_relativity(str(path))
+    r = _cli(["-f", str(path), "--mcmc.input.contiguous", "-K", "8", "-x", "11"])
+    assert r.returncode == 1, r.stderr
+    assert "Set held_out_ratio to default 0.1" in r.stderr
+    assert "start MCMC stochastical" in r.stdout and "MCMC error" in r.stderr
