@@ -368,6 +368,152 @@ def ours_arm(args, net, opts, rank, world, local):
     s.close()
 
 
+# ---------------------------------------------------------------------------
+# time to perplexity
+# ---------------------------------------------------------------------------
+def _gpu_curve(net, opts_kw, pi_dtype, use_graph, iters, interval):
+    """Held-out perplexity every `interval` iterations (before the update,
+    as run() does) against wall time from the start of the loop; state
+    initialisation is outside the clock, as it is outside the reference's
+    run() timer."""
+    import torch
+    from mcmc_for_ammsb_gb300 import MCMCSamplerStochastic, Options, _native
+    o = Options(**dict(opts_kw, pi_dtype=pi_dtype, use_graph=use_graph))
+    s = MCMCSamplerStochastic(o, net).init()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    curve = []
+    done = 0
+    while True:
+        p = s.cal_perplexity_held_out()
+        curve.append((done, time.perf_counter() - t0, p))
+        if done >= iters:
+            break
+        n = min(interval, iters - done)
+        s.step(n)
+        done += n
+    s.close()
+    return curve
+
+
+def _cpu_curve(net, opts_kw, iters, interval):
+    """The oracle's whole-iteration restatement (FP32, reference operation
+    order, one host core) on the same workload, same clock convention."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    K = opts_kw["K"]
+    o = oracle.OracleSampler(net, K, strategy=opts_kw.get("strategy", 0),
+                             mini_batch_size=opts_kw.get("mini_batch_size") or None,
+                             num_node_sample=opts_kw.get("num_node_sample") or None,
+                             alpha=opts_kw.get("alpha", 0.0), epsilon=opts_kw.get("epsilon", 1e-7),
+                             a=opts_kw.get("a", 0.0), b=opts_kw.get("b", 1024.0),
+                             c=opts_kw.get("c", 0.5))
+    rng = np.random.default_rng(0)
+    o.set_state(rng.gamma(1.0, 1.0, (net.N, K)).astype(np.float32),
+                rng.gamma(1.0, 1.0, (K, 2)).astype(np.float32))
+    t0 = time.perf_counter()
+    curve = []
+    done = 0
+    while True:
+        p = o.perplexity("f32")
+        curve.append((done, time.perf_counter() - t0, p))
+        if done >= iters:
+            break
+        for _ in range(min(interval, iters - done)):
+            o.step()
+        done += min(interval, iters - done)
+    return curve
+
+
+def _f64_compare(net, kw, iters, interval):
+    """Perplexity of the FP32 and BF16 device paths against the oracle's FP64
+    restatement of the same iterations (identical draws: the sampling is
+    bit-exact and the noise is the same Philox normals), from one seeded
+    state, every `interval` iterations up to `iters`.  Returns per path the
+    largest relative perplexity error and the curves."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from mcmc_for_ammsb_gb300 import MCMCSamplerStochastic, Options, _native
+    K = kw["K"]
+    rng = np.random.default_rng(0)
+    phi = rng.gamma(1.0, 1.0, (net.N, K)).astype(np.float32)
+    theta = rng.gamma(1.0, 1.0, (K, 2))
+    ref = oracle.OracleSampler64(net, K, strategy=kw.get("strategy", 0),
+                                 mini_batch_size=kw.get("mini_batch_size") or None,
+                                 num_node_sample=kw.get("num_node_sample") or None,
+                                 alpha=kw.get("alpha", 0.0), epsilon=kw.get("epsilon", 1e-7),
+                                 eta0=kw.get("eta0", 1.0), eta1=kw.get("eta1", 1.0),
+                                 a=kw.get("a", 0.0), b=kw.get("b", 1024.0), c=kw.get("c", 0.5))
+    ref.set_state(phi, theta)
+    want = []
+    for it in range(iters + 1):
+        if it % interval == 0:
+            want.append(ref.perplexity())
+        if it < iters:
+            ref.step()
+    out = {}
+    for name, dt in (("f32", _native.PI_F32), ("bf16", _native.PI_BF16)):
+        s = MCMCSamplerStochastic(Options(**dict(kw, pi_dtype=dt)), net).set_state(phi, theta)
+        got = []
+        for it in range(0, iters + 1, interval):
+            got.append(s.cal_perplexity_held_out())
+            if it < iters:
+                s.step(interval)
+        s.close()
+        rel = [abs(g - w) / abs(w) for g, w in zip(got, want)]
+        out[name] = {"max_rel_err": max(rel), "final_rel_err": rel[-1], "perplexity": got}
+    out["f64_oracle"] = {"perplexity": want}
+    return out
+
+
+def _time_to(curve, target):
+    for it, t, p in curve:
+        if p <= target:
+            return t, it
+    return None, None
+
+
+def ttp_arm(args):
+    """Time to held-out perplexity within 1% of the FP32 plain GPU path's
+    final value.  `plain` = FP32 pi with every kernel launched one by one
+    (no CUDA graph); the candidate is BF16 pi, graph-captured."""
+    from mcmc_for_ammsb_gb300 import _native, workloads
+    net, opts = workloads.build(args.workload)
+    keys = ("K", "alpha", "eta0", "eta1", "epsilon", "a", "b", "c", "mini_batch_size",
+            "num_node_sample", "strategy", "held_out_ratio")
+    kw = {k: getattr(opts, k) for k in keys}
+    iters = args.ttp_iters
+    interval = args.ttp_interval
+    runs = {
+        "f32_plain": _gpu_curve(net, kw, _native.PI_F32, 0, iters, interval),
+        "f32_graph": _gpu_curve(net, kw, _native.PI_F32, 1, iters, interval),
+        "bf16_graph": _gpu_curve(net, kw, _native.PI_BF16, 1, iters, interval),
+    }
+    if args.ttp_cpu_iters:
+        runs["cpu_oracle_f32"] = _cpu_curve(net, kw, args.ttp_cpu_iters, interval)
+    f64 = _f64_compare(net, kw, args.ttp_f64_iters, args.ttp_f64_interval) \
+        if args.ttp_f64_iters else None
+    final = runs["f32_plain"][-1][2]
+    target = 1.01 * final
+    out = {}
+    for name, c in runs.items():
+        t, it = _time_to(c, target)
+        out[name] = {"time_to_target_s": t, "iterations_to_target": it,
+                     "final_perplexity": c[-1][2], "iterations": c[-1][0],
+                     "wall_s": c[-1][1], "curve": [(i, round(tt, 4), p) for i, tt, p in c]}
+    base = out["f32_plain"]["time_to_target_s"]
+    line = {"metric": "time to held-out perplexity within 1% of the FP32 plain GPU path",
+            "workload": args.workload, "N": net.N, "E": net.num_total_edges, "K": opts.K,
+            "target": target, "f32_plain_final": final, "interval": interval,
+            "speedup_bf16_graph_vs_f32_plain":
+                (base / out["bf16_graph"]["time_to_target_s"])
+                if base and out["bf16_graph"]["time_to_target_s"] else None,
+            "runs": out, "vs_fp64": f64}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -384,8 +530,22 @@ def main():
     ap.add_argument("--ref-nodes", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--ttp", action="store_true",
+                    help="time to perplexity (FP32 plain vs BF16 graph-captured) instead of "
+                         "the throughput line")
+    ap.add_argument("--ttp-iters", type=int, default=2000)
+    ap.add_argument("--ttp-interval", type=int, default=100)
+    ap.add_argument("--ttp-cpu-iters", type=int, default=0,
+                    help="also run the oracle's CPU restatement for this many iterations")
+    ap.add_argument("--ttp-f64-iters", type=int, default=0,
+                    help="perplexity error of the FP32/BF16 paths against the FP64 oracle "
+                         "over this many iterations")
+    ap.add_argument("--ttp-f64-interval", type=int, default=50)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.ttp:
+        ttp_arm(args)
+        return
 
     rank, world, local = dist_env()
     if args.impl == "reference" and rank != 0:

@@ -61,6 +61,7 @@ double host_gamma(const Stream& s, uint32_t tag, uint32_t entity, uint64_t idx,
 struct KernelCfg {
   int lpn, vpl, split, npb;  // update_phi
   int tma;                   // wide rows: bulk-copy pipeline kernel
+  int tma_stages;            // its ring depth
   int ppx_lpn, ppx_vpl;      // perplexity
   int kq;                    // commit_beta
 };
@@ -140,12 +141,11 @@ cudaError_t launch_phi_t(ammsb_handle* h, const Buffers& b) {
 }
 
 constexpr int kTmaSplit = 4;
-constexpr int kTmaStages = 4;
 
-template <typename PiT, int VPL>
+template <typename PiT, int VPL, int STAGES, bool FULL>
 cudaError_t launch_phi_tma_t(ammsb_handle* h, const Buffers& b, bool configure) {
-  auto kern = k_update_phi_tma<PiT, VPL, kTmaSplit, kTmaStages>;
-  const size_t smem = PhiTmaSmem<PiT, VPL, kTmaSplit, kTmaStages>::bytes(h->m.Kp, h->m.n_out);
+  auto kern = k_update_phi_tma<PiT, VPL, kTmaSplit, STAGES, FULL>;
+  const size_t smem = PhiTmaSmem<PiT, VPL, kTmaSplit, STAGES>::bytes(h->m.Kp, h->m.n_out);
   if (configure) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -156,13 +156,28 @@ cudaError_t launch_phi_tma_t(ammsb_handle* h, const Buffers& b, bool configure) 
   return cudaGetLastError();
 }
 
+// ring depths the bulk-copy kernel is built for; FULL when every lane's
+// vectors lie inside the row
+template <typename PiT, int VPL>
+cudaError_t launch_phi_tma_v(ammsb_handle* h, const Buffers& b, bool configure) {
+  constexpr int EV = PiTraits<PiT>::kPerVec;
+  const bool full = (h->m.Kp / EV == 32 * VPL);
+#define TMA_CASE(S)                                                                        \
+  if (h->cfg.tma_stages == S)                                                              \
+    return full ? launch_phi_tma_t<PiT, VPL, S, true>(h, b, configure)                     \
+                : launch_phi_tma_t<PiT, VPL, S, false>(h, b, configure);
+  TMA_CASE(3) TMA_CASE(4) TMA_CASE(6)
+#undef TMA_CASE
+  return cudaErrorInvalidConfiguration;
+}
+
 template <typename PiT>
 cudaError_t launch_phi_tma(ammsb_handle* h, const Buffers& b, bool configure) {
   switch (h->cfg.vpl) {
-    case 1: return launch_phi_tma_t<PiT, 1>(h, b, configure);
-    case 2: return launch_phi_tma_t<PiT, 2>(h, b, configure);
-    case 4: return launch_phi_tma_t<PiT, 4>(h, b, configure);
-    case 8: return launch_phi_tma_t<PiT, 8>(h, b, configure);
+    case 1: return launch_phi_tma_v<PiT, 1>(h, b, configure);
+    case 2: return launch_phi_tma_v<PiT, 2>(h, b, configure);
+    case 4: return launch_phi_tma_v<PiT, 4>(h, b, configure);
+    case 8: return launch_phi_tma_v<PiT, 8>(h, b, configure);
     default: return cudaErrorInvalidConfiguration;
   }
 }
@@ -310,8 +325,13 @@ void choose_config(ammsb_handle* h) {
   }
   c.split = (c.lpn == 32) ? (c.vpl >= 2 ? 4 : 2) : 1;
   c.tma = (c.lpn == 32) ? 1 : 0;
+  c.tma_stages = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 4 : 3;  // fastest ring depths on GB300
   if (const char* env = std::getenv("AMMSB_PHI_KERNEL")) {  // "tma" or "regs"
     if (std::strcmp(env, "regs") == 0) c.tma = 0;
+  }
+  if (const char* env = std::getenv("AMMSB_PHI_TMA")) {  // ring stages
+    int st = 0;
+    if (std::sscanf(env, "%d", &st) == 1) c.tma_stages = st;
   }
   c.npb = std::max(1, 128 / (c.lpn * c.split));
   c.ppx_lpn = c.lpn;

@@ -121,31 +121,69 @@ struct PairLoad<__nv_bfloat16> {
   }
 };
 
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Predicated refill (no branch): when pred, arm `bar` for `bytes` and copy
+// `bytes` from global `src` into shared `dst`, completing on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s_if(bool pred, void* dst, const void* src, uint32_t bytes,
+                                                 uint64_t* bar) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %0, 0;\n\t"
+      "@p fence.proxy.async.shared::cta;\n\t"
+      "@p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%1], %4;\n\t"
+      "@p cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%2], [%3], %4, [%1];\n\t}" ::"r"(
+          (int)pred),
+      "r"(smem_addr(bar)), "r"(smem_addr(dst)), "l"(src), "r"(bytes)
+      : "memory");
+}
+
 template <typename PiT, int VPL, int SPLIT, int STAGES>
 struct PhiTmaSmem {
+  // the per-warp A vectors of the epilogue reuse the warp's own ring slice
+  static_assert(STAGES * sizeof(PiT) >= sizeof(float), "ring slice must hold a row of floats");
   static size_t bytes(int Kp, int n_out) {
     size_t ring = (size_t)SPLIT * STAGES * Kp * sizeof(PiT);
     size_t bars = (size_t)SPLIT * STAGES * sizeof(uint64_t);
     size_t w = (size_t)Kp * sizeof(float);
-    size_t A = (size_t)SPLIT * Kp * sizeof(float);
     size_t misc = (size_t)(4 * SPLIT + 8) * sizeof(float) + (size_t)n_out * sizeof(uint32_t);
-    return ring + bars + w + A + misc + 128;
+    return ring + bars + w + misc + 128;
   }
 };
 
-template <typename PiT, int VPL, int SPLIT, int STAGES>
+// One row of the ring as the lane's float pairs (FULL: every lane's vectors
+// lie inside the row).
+template <typename PiT, int VPL, bool FULL>
+__device__ __forceinline__ void load_row_pairs(const PiT* row, int lane, int nvec, f32x2* x2) {
+  constexpr int EV = PiTraits<PiT>::kPerVec;
+#pragma unroll
+  for (int v = 0; v < VPL; ++v) {
+    const int vi = lane + 32 * v;
+    const uint4 raw = (FULL || vi < nvec) ? *reinterpret_cast<const uint4*>(row + vi * EV)
+                                          : make_uint4(0, 0, 0, 0);
+    PairLoad<PiT>::get(raw, x2 + v * (EV / 2));
+  }
+}
+
+// Each warp walks its rows in chunks of STAGES with the ring slot of every
+// row a compile-time constant (the barriers are re-armed from phase 0 at
+// every node), refilling each slot, branch-free, with the row STAGES ahead
+// as soon as the row in it is consumed.
+template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
 __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1) k_update_phi_tma(Model m, Buffers b) {
   using TR = PiTraits<PiT>;
   constexpr int EV = TR::kPerVec;
   constexpr int EPL = VPL * EV;
   constexpr int NT = SPLIT * 32;
+  constexpr int NP = EPL / 2;  // float pairs per lane
   extern __shared__ __align__(128) unsigned char s_raw[];
   const int Kp = m.Kp, K = m.K, n_out = m.n_out;
   PiT* ring = reinterpret_cast<PiT*>(s_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(ring + (size_t)SPLIT * STAGES * Kp);
   float* s_w = reinterpret_cast<float*>(bars + SPLIT * STAGES);
-  float* s_A = s_w + Kp;
-  float* s_red = s_A + (size_t)SPLIT * Kp;  // 4*SPLIT + 8 floats
+  float* s_red = s_w + Kp;  // 4*SPLIT + 8 floats
   uint32_t* s_nb = reinterpret_cast<uint32_t*>(s_red + 4 * SPLIT + 8);
   __shared__ int s_broken;
 
@@ -160,22 +198,39 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
 
   uint64_t* my_bars = bars + warp * STAGES;
   PiT* my_ring = ring + (size_t)warp * STAGES * Kp;
-  if (lane == 0) {
-    for (int s = 0; s < STAGES; ++s) mbar_init(my_bars + s, 1);
-    fence_mbar_init();
-  }
+  float* my_A = reinterpret_cast<float*>(my_ring);  // epilogue: this warp's A (Kp floats)
   if (tid == 0) s_broken = 0;
-  __syncthreads();
-  uint32_t seq = 0;    // rows consumed by this warp so far (barrier phase bookkeeping)
   bool dead = false;   // a bounded wait ran out: this warp issues and waits no more
+  bool armed = false;  // this warp's barriers hold valid mbarrier objects
 
   for (int slot = blockIdx.x; slot < n_nodes; slot += gridDim.x) {
     const int32_t i = b.nodes[slot];
     const float* phi_i = b.phi + (int64_t)i * Kp;
+    const uint32_t* nbr_g = b.nbr + (int64_t)slot * n_out;
+    // rows of this warp: q = warp + SPLIT * t, t < T
+    const int T = (!dead && n_out > warp) ? (n_out - warp + SPLIT - 1) / SPLIT : 0;
+    // (re)arm the barriers at phase 0 and send the first copies before the
+    // node prologue, which they overlap
+    if (lane == 0 && !dead) {
+      for (int s = 0; s < STAGES; ++s) {
+        if (armed) mbar_inval(my_bars + s);
+        mbar_init(my_bars + s, 1);
+      }
+      fence_mbar_init();
+      armed = true;
+      const int pre = T < STAGES ? T : STAGES;
+      for (int t = 0; t < pre; ++t) {
+        const uint32_t j = nbr_g[warp + SPLIT * t] & 0x7fffffffu;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(my_bars + t, row_bytes);
+        bulk_copy_g2s(my_ring + (size_t)t * Kp, pi + (int64_t)j * Kp, row_bytes, my_bars + t);
+      }
+    }
+    __syncwarp();
     // ---- node prologue: S = sum phi, s_i = sum pi, w = pi * (beta - eps)
     float S = 0.f;
     for (int k = tid; k < Kp; k += NT) S += phi_i[k];
-    for (int q = tid; q < n_out; q += NT) s_nb[q] = b.nbr[(int64_t)slot * n_out + q];
+    for (int q = tid; q < n_out; q += NT) s_nb[q] = nbr_g[q];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
     if (lane == 0) s_red[warp] = S;
@@ -197,112 +252,92 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
 #pragma unroll
     for (int w = 0; w < SPLIT; ++w) si += s_red[SPLIT + w];
     const float one_m_si = 1.0f - si;
+    const float eps_y1 = m.epsilon, eps_y0 = 1.0f - m.epsilon;
 
-    // ---- rows of this warp: q = warp + SPLIT * t
-    const int T = (!dead && n_out > warp) ? (n_out - warp + SPLIT - 1) / SPLIT : 0;
-    constexpr int NP = EPL / 2;  // float pairs per lane
     f32x2 w2[NP], A2[NP];
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
       const int vi = lane + 32 * v;
 #pragma unroll
       for (int e = 0; e < EV; e += 2) {
-        const float lo = (vi < nvec) ? s_w[vi * EV + e] : 0.f;
-        const float hi = (vi < nvec) ? s_w[vi * EV + e + 1] : 0.f;
+        const float lo = (FULL || vi < nvec) ? s_w[vi * EV + e] : 0.f;
+        const float hi = (FULL || vi < nvec) ? s_w[vi * EV + e + 1] : 0.f;
         w2[(v * EV + e) / 2] = pack_f32x2(lo, hi);
         A2[(v * EV + e) / 2] = pack_f32x2(0.f, 0.f);
       }
     }
-    if (lane == 0) {
-      const int pre = T < STAGES ? T : STAGES;
-      for (int t = 0; t < pre; ++t) {
-        const uint32_t sq = seq + t;
-        const int stg = sq % STAGES;
-        const uint32_t j = s_nb[warp + SPLIT * t] & 0x7fffffffu;
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(my_bars + stg, row_bytes);
-        bulk_copy_g2s(my_ring + (size_t)stg * Kp, pi + (int64_t)j * Kp, row_bytes, my_bars + stg);
-      }
-    }
     float Bsum = 0.f;
-    bool broken = false;
-    int t = 0;
-    for (; t < T; ++t) {
-      const uint32_t sq = seq + t;
-      const int stg = sq % STAGES;
-      if (!mbar_wait_bounded(my_bars + stg, (sq / STAGES) & 1u)) {
-        broken = true;
-        break;
-      }
-      const PiT* row = my_ring + (size_t)stg * Kp;
-      // the lane's slice of the row as float pairs, loaded once for both passes
-      f32x2 x2[NP];
+    int t_fail = -1;
+    for (int t0 = 0; t0 < T && t_fail < 0; t0 += STAGES) {
+      const uint32_t par = (uint32_t)(t0 / STAGES) & 1u;
 #pragma unroll
-      for (int v = 0; v < VPL; ++v) {
-        const int vi = lane + 32 * v;
-        const uint4 raw = (vi < nvec) ? *reinterpret_cast<const uint4*>(row + vi * EV)
-                                      : make_uint4(0, 0, 0, 0);
-        PairLoad<PiT>::get(raw, x2 + v * (EV / 2));
-      }
-      // four independent pair accumulators break the FMA dependency chain
-      f32x2 d2[4] = {0ull, 0ull, 0ull, 0ull};
+      for (int u = 0; u < STAGES; ++u) {
+        const int t = t0 + u;
+        if (t >= T) break;
+        if (!mbar_wait_bounded(my_bars + u, par)) {
+          t_fail = t;
+          break;
+        }
+        const PiT* row = my_ring + (size_t)u * Kp;
+        f32x2 x2[NP];
+        load_row_pairs<PiT, VPL, FULL>(row, lane, nvec, x2);
+        // four independent pair accumulators break the FMA dependency chain
+        f32x2 d2[4] = {0ull, 0ull, 0ull, 0ull};
 #pragma unroll
-      for (int e = 0; e < NP; ++e) d2[e & 3] = fma_f32x2(w2[e], x2[e], d2[e & 3]);
-      float D;
-      {
-        float a0, a1, b0, b1, c0, c1, e0, e1;
-        unpack_f32x2(d2[0], a0, a1);
-        unpack_f32x2(d2[1], b0, b1);
-        unpack_f32x2(d2[2], c0, c1);
-        unpack_f32x2(d2[3], e0, e1);
-        D = ((a0 + a1) + (b0 + b1)) + ((c0 + c1) + (e0 + e1));
-      }
+        for (int e = 0; e < NP; ++e) d2[e & 3] = fma_f32x2(w2[e], x2[e], d2[e & 3]);
+        float D;
+        {
+          float a0, a1, b0, b1, c0, c1, e0, e1;
+          unpack_f32x2(d2[0], a0, a1);
+          unpack_f32x2(d2[1], b0, b1);
+          unpack_f32x2(d2[2], c0, c1);
+          unpack_f32x2(d2[3], e0, e1);
+          D = ((a0 + a1) + (b0 + b1)) + ((c0 + c1) + (e0 + e1));
+        }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) D += __shfl_xor_sync(0xffffffffu, D, o);
-      const uint32_t word = s_nb[warp + SPLIT * t];
-      const bool y = (word >> 31) != 0;
-      const float sgn = y ? 1.f : -1.f;
-      const float ej = y ? m.epsilon : 1.0f - m.epsilon;
-      const float P = fmaf(sgn, D, ej * si);
-      const float invP = __frcp_rn(P);
-      const float cj = sgn * invP;
-      Bsum += (ej * one_m_si - sgn * D) * invP;
-      const f32x2 c2 = pack_f32x2(cj, cj);
+        for (int o = 16; o > 0; o >>= 1) D += __shfl_xor_sync(0xffffffffu, D, o);
+        const uint32_t word = s_nb[warp + SPLIT * t];
+        const bool y = (word >> 31) != 0;
+        const float sgn = y ? 1.f : -1.f;
+        const float ej = y ? eps_y1 : eps_y0;
+        const float P = fmaf(sgn, D, ej * si);
+        const float invP = __frcp_rn(P);
+        const float cj = sgn * invP;
+        Bsum += (ej * one_m_si - sgn * D) * invP;
+        const f32x2 c2 = pack_f32x2(cj, cj);
 #pragma unroll
-      for (int e = 0; e < NP; ++e) A2[e] = fma_f32x2(c2, x2[e], A2[e]);
-      __syncwarp();
-      if (lane == 0 && t + STAGES < T) {  // refill this stage with row t + STAGES
-        const uint32_t j = s_nb[warp + SPLIT * (t + STAGES)] & 0x7fffffffu;
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(my_bars + stg, row_bytes);
-        bulk_copy_g2s(my_ring + (size_t)stg * Kp, pi + (int64_t)j * Kp, row_bytes, my_bars + stg);
+        for (int e = 0; e < NP; ++e) A2[e] = fma_f32x2(c2, x2[e], A2[e]);
+        __syncwarp();
+        // refill slot u with row t + STAGES once every lane has read row t
+        const int tn = t + STAGES;
+        const uint32_t jn = (tn < T) ? (s_nb[warp + SPLIT * tn] & 0x7fffffffu) : 0u;
+        bulk_copy_g2s_if(lane == 0 && tn < T, my_ring + (size_t)u * Kp, pi + (int64_t)jn * Kp, row_bytes,
+                         my_bars + u);
       }
     }
-    if (broken) {
-      // drain the copies still in flight for rows t .. min(T, t+STAGES)-1
+    if (t_fail >= 0) {
+      // drain the copies still in flight: rows t_fail .. min(T, t_fail + STAGES) - 1
       dead = true;
-      const int last = (T < t + STAGES) ? T : t + STAGES;
-      for (int u = t; u < last; ++u) {
-        const uint32_t sq = seq + u;
-        mbar_wait_bounded(my_bars + sq % STAGES, (sq / STAGES) & 1u);
-      }
+      const int last = (T < t_fail + STAGES) ? T : t_fail + STAGES;
+      for (int u = t_fail; u < last; ++u)
+        mbar_wait_bounded(my_bars + (u % STAGES), (uint32_t)(u / STAGES) & 1u);
       if (lane == 0) {
         atomicOr(&b.gc->err, kErrPipeline);
         s_broken = 1;
       }
     }
-    seq += T;
-    // ---- publish A, B; epilogue over all NT threads
+    __syncwarp();
+    // ---- publish A (into this warp's own ring slice, now idle) and B
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
       const int vi = lane + 32 * v;
-      if (vi < nvec) {
+      if (FULL || vi < nvec) {
 #pragma unroll
         for (int e = 0; e < EV; e += 2) {
           float lo, hi;
           unpack_f32x2(A2[(v * EV + e) / 2], lo, hi);
-          s_A[(size_t)warp * Kp + vi * EV + e] = lo;
-          s_A[(size_t)warp * Kp + vi * EV + e + 1] = hi;
+          my_A[vi * EV + e] = lo;
+          my_A[vi * EV + e + 1] = hi;
         }
       }
     }
@@ -310,7 +345,7 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
     __syncthreads();
     float Bt = 0.f;
 #pragma unroll
-    for (int w2 = 0; w2 < SPLIT; ++w2) Bt += s_red[2 * SPLIT + w2];
+    for (int w2i = 0; w2i < SPLIT; ++w2i) Bt += s_red[2 * SPLIT + w2i];
     const float invS = 1.0f / S;
     const float half_eps = eps_t / 2.0f;
     const bool write = (s_broken == 0);
@@ -349,7 +384,8 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
         if (k < K) {
           float Ak = 0.f;
 #pragma unroll
-          for (int s = 0; s < SPLIT; ++s) Ak += s_A[(size_t)s * Kp + k];
+          for (int s = 0; s < SPLIT; ++s)
+            Ak += reinterpret_cast<const float*>(ring + (size_t)s * STAGES * Kp)[k];
           const float bk = b.beta[k] - m.epsilon;
           const float grad = (bk * Ak + Bt) * invS;
           const float ph = phi_i[k];
@@ -367,7 +403,7 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
     __syncthreads();
     Snew = 0.f;
 #pragma unroll
-    for (int w2 = 0; w2 < SPLIT; ++w2) Snew += s_red[3 * SPLIT + w2];
+    for (int w2i = 0; w2i < SPLIT; ++w2i) Snew += s_red[3 * SPLIT + w2i];
     float* st = b.stage + (int64_t)slot * Kp;
 #pragma unroll
     for (int g = 0; g < NG; ++g) {

@@ -457,3 +457,79 @@ int oracle_step_f32(const oracle_params *p, const oracle_graph *g,
   free(nodes);
   return rc;
 }
+
+/* The same iteration in double: identical draws (the minibatch, the
+ * neighbour sets and the float normals of the Philox spec, widened), double
+ * arithmetic throughout, eps_t in double.  The FP64 trajectory reference of
+ * the FP32 and BF16 device paths. */
+int oracle_step_f64(const oracle_params *p, const oracle_graph *g,
+                    uint32_t step, double *pi, double *phi, double *theta,
+                    double *beta, oracle_mb_info *info) {
+  const int32_t K = p->K;
+  int64_t max_edges = p->mini_batch_size;
+  for (int64_t v = 0; v < g->n; ++v) {
+    int64_t d = g->row_ptr[v + 1] - g->row_ptr[v];
+    if (d > max_edges) max_edges = d;
+  }
+  int32_t *ea = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
+  int32_t *eb = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
+  uint8_t *ey = (uint8_t *)malloc((size_t)max_edges);
+  int32_t *nodes = (int32_t *)malloc(sizeof(int32_t) * (size_t)(max_edges + 1));
+  int rc = oracle_sample_minibatch(g, p->strategy, p->mini_batch_size,
+                                   p->num_total_edges, p->seed, p->chain, step,
+                                   ea, eb, ey, (int32_t)max_edges, nodes,
+                                   (int32_t)(max_edges + 1), info);
+  if (rc != 0) {
+    free(ea); free(eb); free(ey); free(nodes);
+    return rc;
+  }
+  const double eps_t = p->a * pow(1.0 + (double)step / p->b, -p->c);
+  const int32_t n_out = (int32_t)p->num_node_sample + 1;
+  int32_t *nb = (int32_t *)malloc(sizeof(int32_t) * (size_t)n_out);
+  uint8_t *ny = (uint8_t *)malloc((size_t)n_out);
+  double *noise = (double *)malloc(sizeof(double) * (size_t)K);
+  for (int32_t s = 0; s < info->n_nodes && rc == 0; ++s) {
+    const int32_t i = nodes[s];
+    if (oracle_sample_neighbors(g, i, n_out, p->seed, p->chain, step, nb, ny) < 0) {
+      rc = -4;
+      break;
+    }
+    for (int32_t k = 0; k < K; ++k)
+      noise[k] = (double)oracle_normal(p->seed, p->chain, OR_P_PHI_NOISE,
+                                       (uint32_t)i, step, (uint64_t)k);
+    oracle_update_phi_f64(K, pi, phi + (int64_t)i * K, i, nb, ny, n_out, beta,
+                          (double)p->alpha, (double)p->epsilon, eps_t, p->N,
+                          p->num_node_sample, noise);
+  }
+  if (rc == 0) {
+    for (int32_t s = 0; s < info->n_nodes; ++s) {
+      const int32_t i = nodes[s];
+      oracle_normalize_f64(K, phi + (int64_t)i * K, pi + (int64_t)i * K);
+    }
+    int32_t *va = (int32_t *)malloc(sizeof(int32_t) * (size_t)(info->n_edges + 1));
+    int32_t *vb = (int32_t *)malloc(sizeof(int32_t) * (size_t)(info->n_edges + 1));
+    for (int32_t e = 0; e < info->n_edges; ++e) {
+      va[e] = nodes[ea[e]];
+      vb[e] = nodes[eb[e]];
+    }
+    double *tn = (double *)malloc(sizeof(double) * 2 * (size_t)K);
+    for (int32_t k = 0; k < 2 * K; ++k)
+      tn[k] = (double)oracle_normal(p->seed, p->chain, OR_P_THETA_NOISE, 0,
+                                    step, (uint64_t)k);
+    const double eta[2] = {(double)p->eta0, (double)p->eta1};
+    oracle_update_beta_f64(K, pi, va, vb, ey, info->n_edges, theta, beta, eta,
+                           (double)p->epsilon, eps_t, (double)info->scale, tn,
+                           NULL);
+    free(tn);
+    free(va);
+    free(vb);
+  }
+  free(noise);
+  free(nb);
+  free(ny);
+  free(ea);
+  free(eb);
+  free(ey);
+  free(nodes);
+  return rc;
+}

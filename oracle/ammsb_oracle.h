@@ -195,6 +195,11 @@ typedef struct {
 int oracle_step_f32(const oracle_params *p, const oracle_graph *g,
                     uint32_t step, float *pi, float *phi, float *theta,
                     float *beta, oracle_mb_info *info);
+/* The same iteration in double (same draws, eps_t in double): the FP64
+ * trajectory reference. */
+int oracle_step_f64(const oracle_params *p, const oracle_graph *g,
+                    uint32_t step, double *pi, double *phi, double *theta,
+                    double *beta, oracle_mb_info *info);
 
 #ifdef __cplusplus
 }

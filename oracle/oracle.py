@@ -80,6 +80,7 @@ def lib():
         L.oracle_perplexity_f64.restype = ctypes.c_double
         L.oracle_perplexity_f64acc.restype = ctypes.c_double
         L.oracle_step_f32.restype = ctypes.c_int
+        L.oracle_step_f64.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -294,5 +295,33 @@ class OracleSampler:
     def perplexity(self, mode="f64acc"):
         v = perplexity(self.K, self.pi, self.network.held_out, self.beta, self.p.epsilon,
                        self.ppx, self.average_count, mode)
+        self.average_count += 1
+        return v
+
+
+class OracleSampler64(OracleSampler):
+    """The same whole-iteration sampler in double arithmetic with the same
+    draws: the FP64 trajectory reference of the FP32 and BF16 device paths."""
+
+    def set_state(self, phi, theta):
+        self.phi = np.ascontiguousarray(phi, np.float64).copy()
+        self.theta = np.ascontiguousarray(theta, np.float64).copy()
+        self.beta = self.theta[:, 1] / (self.theta[:, 0] + self.theta[:, 1])
+        self.pi = normalize(self.phi, np.float64)
+        self.ppx = np.zeros(self.network.held_out[0].shape[0], np.float64)
+
+    def step(self):
+        info = MbInfo()
+        rc = lib().oracle_step_f64(ctypes.byref(self.p), ctypes.byref(self.og.g),
+                                   ctypes.c_uint32(self.step_count), _p(self.pi), _p(self.phi),
+                                   _p(self.theta), _p(self.beta), ctypes.byref(info))
+        if rc != 0:
+            raise RuntimeError("oracle step failed: %d" % rc)
+        self.step_count += 1
+        return info
+
+    def perplexity(self, mode="f64"):
+        v = perplexity(self.K, self.pi, self.network.held_out, self.beta, self.p.epsilon,
+                       self.ppx, self.average_count, "f64")
         self.average_count += 1
         return v

@@ -1,0 +1,54 @@
+"""Perplexity of the FP32 and BF16 device paths against an FP64 trajectory.
+
+The FP64 reference is the oracle's double-precision restatement of the same
+iterations (oracle_step_f64): the minibatches and neighbour sets are the
+spec's (bit-exact on the device) and the noise is the same Philox normals,
+so the trajectories differ by rounding alone.  On the small workload
+(N=5,000, K=32) from one seeded state, every 50 iterations up to 300:
+  FP32 pi: relative perplexity error <= 2e-3;
+  BF16 pi: relative perplexity error <= 5e-3.
+Rounding differences feed back through the chain (the noise is scaled by
+sqrt(phi), the step reflects at zero), so the gap grows with the
+iterations: on GB300 it was ~7e-4 (FP32) and ~1.2e-3 (BF16) after 500
+iterations of this workload, and ~1.5e-4 on the 100,000-node one.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mcmc_for_ammsb_gb300 import MCMCSamplerStochastic, Options, _native, workloads
+
+pytestmark = pytest.mark.gpu
+
+ITERS, EVERY = 300, 50
+TOL = {_native.PI_F32: 2e-3, _native.PI_BF16: 5e-3}
+
+
+def test_perplexity_against_fp64_trajectory(native_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    net, opts = workloads.build("small")
+    K = 32
+    kw = dict(K=K, num_node_sample=32, a=0.01, b=1024.0, c=0.55)
+    rng = np.random.default_rng(5)
+    phi = rng.gamma(1.0, 1.0, (net.N, K)).astype(np.float32)
+    theta = rng.gamma(1.0, 1.0, (K, 2))
+    ref = oracle.OracleSampler64(net, K, num_node_sample=32, a=0.01, b=1024.0, c=0.55)
+    ref.set_state(phi, theta)
+    want = []
+    for it in range(ITERS + 1):
+        if it % EVERY == 0:
+            want.append(ref.perplexity())
+        if it < ITERS:
+            ref.step()
+    for dt, tol in TOL.items():
+        s = MCMCSamplerStochastic(Options(**dict(kw, pi_dtype=dt)), net).set_state(phi, theta)
+        got = []
+        for it in range(0, ITERS + 1, EVERY):
+            got.append(s.cal_perplexity_held_out())
+            if it < ITERS:
+                s.step(EVERY)
+        s.close()
+        rel = np.abs(np.array(got) - np.array(want)) / np.abs(np.array(want))
+        assert rel.max() <= tol, (dt, rel)
