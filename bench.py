@@ -514,6 +514,76 @@ def ttp_arm(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# many chains: one launch per iteration for all of them
+# ---------------------------------------------------------------------------
+def chains_arm(args):
+    """The batching workload: args.chains independent chains, each on its own
+    synthetic graph from seed i (N log-uniform in [1,000, 50,000], intra
+    degree 6, K in {16, 32, 64, 128}, minibatch 32..1024, 32 neighbours,
+    BF16 pi), advanced as one batch (one CUDA graph launch per iteration for
+    all chains), against the same chains stepped one after another with
+    their own per-chain graphs."""
+    import torch
+    from mcmc_for_ammsb_gb300 import ChainBatch, MCMCSamplerStochastic, Network, Options, workloads
+    samplers, configs = [], []
+    for i in range(args.chains):
+        w = workloads.chain_workload(i)
+        net = Network.synthetic(**w["gen"])
+        net.make_held_out(w["opts"]["held_out_ratio"], seed=w["gen"]["seed"])
+        s = MCMCSamplerStochastic(Options(**w["opts"]), net).init()
+        if not args.no_autotune:
+            configs.append(s.autotune(reps=5))
+        samplers.append(s)
+    batch = ChainBatch(samplers)
+    stream = torch.cuda.ExternalStream(batch.stream())
+
+    def evals():
+        return sum(s.counters()[0] for s in samplers)
+
+    batch.step(args.warmup)
+    torch.cuda.synchronize()
+    e0 = evals()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    batch.step(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    e1 = evals()
+    # the same chains without the batch: every chain runs its own graph on
+    # its own stream (all streams queued at once, so the GPU runs them side
+    # by side), host clock around all of them
+    for s in samplers:
+        s.step(args.warmup)
+    torch.cuda.synchronize()
+    e2 = evals()
+    t0 = time.perf_counter()
+    for s in samplers:
+        s.step(args.steps)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    e3 = evals()
+    Ks = sorted({s.K for s in samplers})
+    line = {"metric": "edge-evals/s, %d independent chains, one graph launch per iteration" % args.chains,
+            "value": (e1 - e0) / (ms / 1000.0), "unit": UNIT,
+            "ms_per_iteration_all_chains": ms / args.steps,
+            "chain_iterations_per_s": args.chains * args.steps / (ms / 1000.0),
+            "per_chain_streams_value": (e3 - e2) / seq_s,
+            "per_chain_streams_ms_per_iteration_all_chains": 1000.0 * seq_s / args.steps,
+            "update_phi_launches_per_iteration": batch.groups(),
+            "chains": args.chains, "K_values": Ks, "steps": args.steps, "warmup": args.warmup,
+            "autotuned": not args.no_autotune,
+            "configs": sorted({json.dumps(c, sort_keys=True) for c in configs}),
+            "N_range": [min(s.N for s in samplers), max(s.N for s in samplers)],
+            "dtype": "bf16-pi/f32", "data": "synthetic (planted-community generator, seed i per chain)"}
+    print(json.dumps(line))
+    batch.close()
+    for s in samplers:
+        s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -541,10 +611,16 @@ def main():
                     help="perplexity error of the FP32/BF16 paths against the FP64 oracle "
                          "over this many iterations")
     ap.add_argument("--ttp-f64-interval", type=int, default=50)
+    ap.add_argument("--chains", type=int, default=0,
+                    help="run the batching workload with this many chains instead")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.ttp:
         ttp_arm(args)
+        return
+    if args.chains:
+        chains_arm(args)
         return
 
     rank, world, local = dist_env()

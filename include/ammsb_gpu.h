@@ -192,6 +192,45 @@ void *ammsb_stream(ammsb_handle *h);
 int ammsb_get_counters(ammsb_handle *h, uint64_t *edge_evals,
                        uint64_t *iterations);
 
+/* Autotuner of the update_phi kernel (no reference counterpart): times
+ * every built shape of the kernel that covers this handle's rows -- lanes
+ * per node and vectors per lane (the K-tile), sub-groups per node (warps per
+ * node), and the bulk-copy kernel's ring depth for wide rows -- `reps`
+ * launches each on a non-link minibatch of the handle's own graph against a
+ * scratch copy of phi (the chain's state and its draws are untouched), and
+ * keeps the fastest.  Choices are cached per (device, pi type, row width,
+ * neighbours, minibatch capacity) for the process; AMMSB_TUNE_FRESH times
+ * again.  Needs a state (ammsb_init_state / ammsb_set_state). */
+#define AMMSB_TUNE_FRESH 1
+int ammsb_autotune(ammsb_handle *h, int32_t reps, int32_t flags);
+/* The update_phi configuration in use: out[0..4] = bulk-copy kernel (0/1),
+ * lanes per node, vectors per lane, sub-groups per node, ring depth. */
+int ammsb_get_kernel_config(ammsb_handle *h, int32_t *out);
+
+/* Batches of independent chains (no reference counterpart): the
+ * iterations of many handles -- each with its own graph, held-out set,
+ * state, options and update_phi configuration -- advanced together, one
+ * CUDA graph launch per iteration for all of them.  Each kernel of the
+ * iteration runs once for all chains sharing its compiled shape (the chain
+ * is the grid's y index), so chains of different sizes and row widths take
+ * a handful of launches per iteration instead of five each.  A chain goes
+ * through exactly the states it goes through when stepped on its own (same
+ * kernels, same draws); its step counter advances with the batch.  The
+ * handles must outlive the batch and must not be stepped concurrently with
+ * it; stepping a handle on its own between batch steps is allowed (the
+ * batch then draws again from each chain's own step counter). */
+typedef struct ammsb_batch ammsb_batch;
+int ammsb_batch_create(ammsb_handle *const *handles, int32_t n,
+                       ammsb_batch **out);
+void ammsb_batch_destroy(ammsb_batch *b);
+/* n_iters iterations of every chain (ammsb_step semantics per chain). */
+int ammsb_batch_step(ammsb_batch *b, int64_t n_iters);
+/* Number of update_phi launches per iteration (distinct kernel shapes). */
+int32_t ammsb_batch_groups(const ammsb_batch *b);
+void *ammsb_batch_stream(ammsb_batch *b);
+const char *ammsb_batch_last_error(const ammsb_batch *b);
+const char *ammsb_batch_create_error(void);
+
 /* Checkpoint and resume.  No counterpart in the reference's sequential
  * sampler (its state lives only in memory).  ammsb_save_checkpoint writes
  * the whole chain to `path`: phi, the stored pi bit for bit (F32 or BF16),

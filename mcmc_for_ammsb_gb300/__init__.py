@@ -9,9 +9,9 @@ hand-written sm_103a CUDA kernels behind the C ABI of libammsb_gpu.so
 from . import _native
 from .network import Network
 from .options import Options
-from .sampler import MCMCSamplerStochastic
+from .sampler import ChainBatch, MCMCSamplerStochastic
 
-__all__ = ["Network", "Options", "MCMCSamplerStochastic", "lib"]
+__all__ = ["Network", "Options", "MCMCSamplerStochastic", "ChainBatch", "lib"]
 
 
 def lib():

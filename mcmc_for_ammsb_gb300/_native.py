@@ -30,6 +30,8 @@ PI_BF16 = 1
 REAL_F32 = 0
 REAL_F64 = 1
 
+TUNE_FRESH = 1
+
 
 class AmmsbOptions(ctypes.Structure):
     _fields_ = [
@@ -131,6 +133,15 @@ SIGNATURES = [
     ("ammsb_profile_step", ctypes.c_int, [_P, _F64P]),
     ("ammsb_stream", _P, [_P]),
     ("ammsb_get_counters", ctypes.c_int, [_P, _U64P, _U64P]),
+    ("ammsb_autotune", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    ("ammsb_get_kernel_config", ctypes.c_int, [_P, _I32P]),
+    ("ammsb_batch_create", ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int32, ctypes.POINTER(_P)]),
+    ("ammsb_batch_destroy", None, [_P]),
+    ("ammsb_batch_step", ctypes.c_int, [_P, ctypes.c_int64]),
+    ("ammsb_batch_groups", ctypes.c_int32, [_P]),
+    ("ammsb_batch_stream", _P, [_P]),
+    ("ammsb_batch_last_error", ctypes.c_char_p, [_P]),
+    ("ammsb_batch_create_error", ctypes.c_char_p, []),
     ("ammsb_save_checkpoint", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("ammsb_load_checkpoint", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("ammsb_perplexity_noalloc", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,

@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libammsb_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-Wall", "-diag-suppress", "177"]
-SOURCES = ["ammsb_gpu.cu", "ammsb_host.cpp", "ammsb_noalloc.cu", "ammsb_adjoint.cu"]
+SOURCES = ["ammsb_gpu.cu", "ammsb_batch.cu", "ammsb_host.cpp", "ammsb_noalloc.cu", "ammsb_adjoint.cu"]
 
 
 def _nvcc():

@@ -12,14 +12,14 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
-#include "../../include/ammsb_gpu.h"
-#include "ammsb_kernels.cuh"
+#include "ammsb_internal.h"
 #include "ammsb_phi_tma.cuh"
-
-using namespace ammsb;
 
 namespace {
 thread_local std::string g_create_error;
@@ -58,64 +58,6 @@ double host_gamma(const Stream& s, uint32_t tag, uint32_t entity, uint64_t idx,
 
 }  // namespace
 
-struct KernelCfg {
-  int lpn, vpl, split, npb;  // update_phi
-  int tma;                   // wide rows: bulk-copy pipeline kernel
-  int tma_stages;            // its ring depth
-  int ppx_lpn, ppx_vpl;      // perplexity
-  int kq;                    // commit_beta
-};
-
-struct ammsb_handle {
-  ammsb_options opt{};
-  int device = 0;
-  cudaStream_t stream = nullptr;  // the handle's stream: updates, perplexity, copies
-  cudaStream_t side = nullptr;    // draws of the next iteration, overlapped with the update
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  Model m{};
-  DevGraph g{};
-  Buffers b{};        // shared state pointers (bufs[p] add the minibatch buffers)
-  Buffers bufs[2]{};  // ping-pong minibatch buffer sets
-  DevCounters* gc = nullptr;
-  int parity = 0;           // buffer set of the next iteration
-  bool prefetched = false;  // bufs[parity] already holds the next iteration's draws
-  int last = -1;            // buffer set of the last applied iteration
-  KernelCfg cfg{};
-  int64_t E = 0, H = 0, T = 0;
-  int pi_bytes = 4;
-  // device allocations
-  std::vector<void*> allocs;
-  int32_t* d_ha = nullptr;
-  int32_t* d_hb = nullptr;
-  uint8_t* d_hy = nullptr;
-  float* d_ppx = nullptr;
-  double* d_ppx_part = nullptr;
-  double* d_ppx_out = nullptr;
-  int ppx_blocks = 1;
-  float* d_fed_phi_noise = nullptr;
-  float* d_fed_theta_noise = nullptr;
-  int32_t* d_err_init = nullptr;
-  int ncommit = 1;
-  int nbr_blocks = 1, phi_blocks = 1;
-  size_t phi_smem = 0, nbr_smem = 0, mb_smem = 0;
-  // host mirrors
-  uint64_t step_count = 1;     // learner.cc:37
-  uint64_t average_count = 1;  // learner.cc:30
-  std::vector<double> ppx_history;
-  bool state_ready = false;
-  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
-  std::string err;
-};
-
-#define CK(call)                                                              \
-  do {                                                                        \
-    cudaError_t e_ = (call);                                                  \
-    if (e_ != cudaSuccess) {                                                  \
-      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
-      return AMMSB_E_CUDA;                                                    \
-    }                                                                         \
-  } while (0)
-
 namespace {
 
 template <typename T>
@@ -147,7 +89,7 @@ cudaError_t launch_phi_tma_t(ammsb_handle* h, const Buffers& b, bool configure) 
   auto kern = k_update_phi_tma<PiT, VPL, kTmaSplit, STAGES, FULL>;
   const size_t smem = PhiTmaSmem<PiT, VPL, kTmaSplit, STAGES>::bytes(h->m.Kp, h->m.n_out);
   if (configure) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ammsb_detail::raise_smem_limit(kern, smem);
     if (e != cudaSuccess) return e;
     h->phi_smem = smem;
     return cudaSuccess;
@@ -166,7 +108,7 @@ cudaError_t launch_phi_tma_v(ammsb_handle* h, const Buffers& b, bool configure) 
   if (h->cfg.tma_stages == S)                                                              \
     return full ? launch_phi_tma_t<PiT, VPL, S, true>(h, b, configure)                     \
                 : launch_phi_tma_t<PiT, VPL, S, false>(h, b, configure);
-  TMA_CASE(3) TMA_CASE(4) TMA_CASE(6)
+  AMMSB_PHI_TMA_STAGES(TMA_CASE)
 #undef TMA_CASE
   return cudaErrorInvalidConfiguration;
 }
@@ -188,11 +130,7 @@ cudaError_t launch_phi(ammsb_handle* h, const Buffers& b) {
   if (c.tma) return launch_phi_tma<PiT>(h, b, false);
 #define PHI_CASE(L, V, S) \
   if (c.lpn == L && c.vpl == V && c.split == S) return launch_phi_t<PiT, L, V, S>(h, b);
-  PHI_CASE(1, 1, 1) PHI_CASE(2, 1, 1) PHI_CASE(4, 1, 1) PHI_CASE(8, 1, 1) PHI_CASE(16, 1, 1)
-  PHI_CASE(32, 1, 1) PHI_CASE(32, 1, 2) PHI_CASE(32, 1, 4)
-  PHI_CASE(32, 2, 1) PHI_CASE(32, 2, 2) PHI_CASE(32, 2, 4)
-  PHI_CASE(32, 4, 1) PHI_CASE(32, 4, 2) PHI_CASE(32, 4, 4)
-  PHI_CASE(32, 8, 1) PHI_CASE(32, 8, 2) PHI_CASE(32, 8, 4)
+  AMMSB_PHI_REG_SHAPES(PHI_CASE)
 #undef PHI_CASE
   return cudaErrorInvalidConfiguration;
 }
@@ -341,6 +279,11 @@ void choose_config(ammsb_handle* h) {
 }
 
 }  // namespace
+
+namespace ammsb_detail {
+int check_device_err(ammsb_handle* h) { return ::check_device_err(h); }
+int invalidate_prefetch(ammsb_handle* h) { return ::invalidate_prefetch(h); }
+}  // namespace ammsb_detail
 
 extern "C" {
 
@@ -599,15 +542,16 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
     TRY(dev_alloc(h, &bp.nbr, (size_t)m.max_nodes * m.n_out));
     TRY(dev_alloc(h, &bp.st, 1));
   }
-  TRY(dev_alloc(h, &b.cand, (size_t)o.mini_batch_size));
-  const int hcap = next_pow2(std::max<int64_t>(64, 2 * o.mini_batch_size));
+  // a minibatch round examines up to max(remaining, 4096) candidates while
+  // the dedup hash stays at most half full
+  TRY(dev_alloc(h, &b.cand, (size_t)std::max<int64_t>(o.mini_batch_size, 4096)));
+  const int hcap = next_pow2(std::max<int64_t>(8192, 2 * o.mini_batch_size));
   TRY(dev_alloc(h, &b.htab_key, (size_t)hcap));
   TRY(dev_alloc(h, &b.htab_idx, (size_t)hcap));
   b.hmask = (uint32_t)(hcap - 1);
   // the dedup hash lives in shared memory when it fits (up to 16Ki entries)
   if (hcap <= 16384 &&
-      cudaFuncSetAttribute(k_sample_minibatch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(2 * sizeof(uint32_t) * hcap)) == cudaSuccess)
+      ammsb_detail::raise_smem_limit(k_sample_minibatch, 2 * sizeof(uint32_t) * hcap) == cudaSuccess)
     h->mb_smem = 2 * sizeof(uint32_t) * (size_t)hcap;
   TRY(dev_alloc(h, &b.beta_part, (size_t)m.nbb * 2 * Kp));
   TRY(dev_alloc(h, &h->gc, 1));
@@ -638,8 +582,7 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   h->m.nbr_set_cap = next_pow2(std::max<int64_t>(64, 2 * (int64_t)m.n_out));
   h->nbr_smem = (size_t)8 * h->m.nbr_set_cap * sizeof(int32_t);
   if (h->nbr_smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(k_sample_neighbors<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)h->nbr_smem) != cudaSuccess) {
+    if (ammsb_detail::raise_smem_limit(k_sample_neighbors<8>, h->nbr_smem) != cudaSuccess) {
       h->err = "num_node_sample too large for the neighbour kernel";
       return bail(AMMSB_E_ARG);
     }
@@ -1064,6 +1007,175 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
   h->step_count += 1;
   h->last = h->parity;
   return check_device_err(h);
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner of update_phi: warps-per-node and K-tile.  Every built shape of
+// the kernels that covers this handle's row (lanes x vectors per lane within
+// 2x of the row's 16-byte vectors; the bulk-copy kernel at each ring depth
+// for wide rows) is timed with CUDA events on a non-link minibatch of this
+// handle's graph, against a scratch copy of phi so the chain's state is not
+// touched; the fastest becomes the handle's configuration.  Choices are
+// cached per (device, pi type, row width, neighbours, minibatch capacity).
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, KernelCfg> g_tune_cache;
+
+std::vector<KernelCfg> phi_candidates(const ammsb_handle* h) {
+  const int ev = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 8 : 4;
+  const int nvec = h->m.Kp / ev;
+  std::vector<KernelCfg> out;
+  KernelCfg base = h->cfg;
+  base.tma = 0;
+#define CAND(L, V, S)                                                      \
+  if ((L) * (V) >= nvec && (L) * (V) < 2 * nvec + ((L) == 1 ? 1 : 0)) {  \
+    KernelCfg c = base;                                                    \
+    c.lpn = L;                                                             \
+    c.vpl = V;                                                             \
+    c.split = S;                                                           \
+    out.push_back(c);                                                      \
+  }
+  AMMSB_PHI_REG_SHAPES(CAND)
+#undef CAND
+  if (nvec >= 32) {
+    const int vpl = next_pow2((nvec + 31) / 32);
+    if (vpl <= 8) {
+#define TCAND(S)          \
+  {                       \
+    KernelCfg c = base;   \
+    c.tma = 1;            \
+    c.lpn = 32;           \
+    c.vpl = vpl;          \
+    c.split = 4;          \
+    c.tma_stages = S;     \
+    out.push_back(c);     \
+  }
+      AMMSB_PHI_TMA_STAGES(TCAND)
+#undef TCAND
+    }
+  }
+  return out;
+}
+
+int apply_phi_cfg(ammsb_handle* h, const KernelCfg& c) {
+  h->cfg = c;
+  h->cfg.npb = std::max(1, 128 / (c.lpn * c.split));
+  if (c.tma) {
+    cudaError_t e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_phi_tma<__nv_bfloat16>(h, h->b, true)
+                                                       : launch_phi_tma<float>(h, h->b, true);
+    if (e != cudaSuccess) {
+      h->err = std::string("update_phi configuration: ") + cudaGetErrorString(e);
+      return AMMSB_E_CUDA;
+    }
+  }
+  for (auto& g : h->graph_exec)  // the captured iterations used the old kernels
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  return AMMSB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ammsb_autotune(ammsb_handle* h, int32_t reps, int32_t flags) {
+  if (!h || reps < 1) return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    h->err = "call ammsb_init_state or ammsb_set_state first";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  const auto key = std::make_tuple(h->device, (int)h->opt.pi_dtype, h->m.Kp, h->m.n_out, h->m.max_nodes);
+  if (!(flags & AMMSB_TUNE_FRESH)) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) return apply_phi_cfg(h, it->second);
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  // a non-link minibatch and its neighbour sets into buffer set 0
+  Model mt = h->m;
+  mt.strategy = AMMSB_STRATIFIED_RANDOM_NODE_NONLINKS;
+  const Buffers& b0 = h->bufs[0];
+  k_sample_minibatch<<<1, 1024, h->mb_smem, h->stream>>>(mt, h->g, b0, h->mb_smem > 0);
+  CK(cudaGetLastError());
+  k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, h->stream>>>(h->m, h->g, b0);
+  CK(cudaGetLastError());
+  float* scratch = nullptr;
+  const size_t phi_bytes = sizeof(float) * (size_t)h->m.N * h->m.Kp;
+  CK(cudaMalloc(&scratch, phi_bytes));
+  Buffers bt = b0;
+  bt.phi = scratch;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = AMMSB_OK;
+  const std::vector<KernelCfg> cands = phi_candidates(h);
+  KernelCfg best = h->cfg;
+  float best_ms = 1e30f;
+  auto run = [&]() -> cudaError_t {
+    if (cudaMemcpyAsync(scratch, h->b.phi, phi_bytes, cudaMemcpyDeviceToDevice, h->stream) ||
+        cudaEventCreate(&e0) || cudaEventCreate(&e1))
+      return cudaGetLastError();
+    for (const KernelCfg& c : cands) {
+      if (apply_phi_cfg(h, c) != AMMSB_OK) continue;  // shape not launchable here
+      auto launch = [&]() {
+        return (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_phi<__nv_bfloat16>(h, bt)
+                                                  : launch_phi<float>(h, bt);
+      };
+      cudaError_t e = launch();  // warm-up
+      if (e != cudaSuccess) return e;
+      if ((e = cudaEventRecord(e0, h->stream)) != cudaSuccess) return e;
+      for (int r = 0; r < reps; ++r)
+        if ((e = launch()) != cudaSuccess) return e;
+      if ((e = cudaEventRecord(e1, h->stream)) != cudaSuccess) return e;
+      if ((e = cudaEventSynchronize(e1)) != cudaSuccess) return e;
+      float ms = 0.f;
+      if ((e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) return e;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+    return cudaSuccess;
+  };
+  cudaError_t e = run();
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(h->stream);
+  cudaFree(scratch);
+  if (e != cudaSuccess) {
+    h->err = std::string("autotune: ") + cudaGetErrorString(e);
+    rc = AMMSB_E_CUDA;
+  }
+  // the tuning draws are not an iteration: the next draw is step_count's
+  const uint32_t s = (uint32_t)h->step_count;
+  CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+  h->prefetched = false;
+  h->parity = 0;
+  h->last = -1;
+  int rc2 = apply_phi_cfg(h, best);
+  CK(cudaStreamSynchronize(h->stream));
+  if (rc) return rc;
+  if (rc2) return rc2;
+  rc = ammsb_detail::check_device_err(h);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache[key] = best;
+  return AMMSB_OK;
+}
+
+int ammsb_get_kernel_config(ammsb_handle* h, int32_t* out) {
+  if (!h || !out) return AMMSB_E_ARG;
+  out[0] = h->cfg.tma;
+  out[1] = h->cfg.lpn;
+  out[2] = h->cfg.vpl;
+  out[3] = h->cfg.split;
+  out[4] = h->cfg.tma_stages;
+  return AMMSB_OK;
 }
 
 void* ammsb_stream(ammsb_handle* h) { return h ? (void*)h->stream : nullptr; }

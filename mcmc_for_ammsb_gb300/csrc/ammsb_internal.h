@@ -1,0 +1,111 @@
+// ammsb_internal.h -- the sampler handle and the helpers shared by the
+// host-side translation units (ammsb_gpu.cu: one chain; ammsb_batch.cu:
+// many chains per launch).  Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ammsb_gpu.h"
+#include "ammsb_kernels.cuh"
+
+using namespace ammsb;
+
+struct KernelCfg {
+  int lpn, vpl, split, npb;  // update_phi
+  int tma;                   // wide rows: bulk-copy pipeline kernel
+  int tma_stages;            // its ring depth
+  int ppx_lpn, ppx_vpl;      // perplexity
+  int kq;                    // commit_beta
+};
+
+struct ammsb_handle {
+  ammsb_options opt{};
+  int device = 0;
+  cudaStream_t stream = nullptr;  // the handle's stream: updates, perplexity, copies
+  cudaStream_t side = nullptr;    // draws of the next iteration, overlapped with the update
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  Model m{};
+  DevGraph g{};
+  Buffers b{};        // shared state pointers (bufs[p] add the minibatch buffers)
+  Buffers bufs[2]{};  // ping-pong minibatch buffer sets
+  DevCounters* gc = nullptr;
+  int parity = 0;           // buffer set of the next iteration
+  bool prefetched = false;  // bufs[parity] already holds the next iteration's draws
+  int last = -1;            // buffer set of the last applied iteration
+  KernelCfg cfg{};
+  int64_t E = 0, H = 0, T = 0;
+  int pi_bytes = 4;
+  // device allocations
+  std::vector<void*> allocs;
+  int32_t* d_ha = nullptr;
+  int32_t* d_hb = nullptr;
+  uint8_t* d_hy = nullptr;
+  float* d_ppx = nullptr;
+  double* d_ppx_part = nullptr;
+  double* d_ppx_out = nullptr;
+  int ppx_blocks = 1;
+  float* d_fed_phi_noise = nullptr;
+  float* d_fed_theta_noise = nullptr;
+  int32_t* d_err_init = nullptr;
+  int ncommit = 1;
+  int nbr_blocks = 1, phi_blocks = 1;
+  size_t phi_smem = 0, nbr_smem = 0, mb_smem = 0;
+  // host mirrors
+  uint64_t step_count = 1;     // learner.cc:37
+  uint64_t average_count = 1;  // learner.cc:30
+  std::vector<double> ppx_history;
+  bool state_ready = false;
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  std::string err;
+};
+
+#define CK(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return AMMSB_E_CUDA;                                                    \
+    }                                                                         \
+  } while (0)
+
+// Shapes of the register-path update_phi kernel that are built: (lanes per
+// node, 16-byte vectors per lane, sub-groups splitting the neighbours).  The
+// lanes x vectors product is the K-tile a node's row is cut into; lanes x
+// split is the number of threads (warps-per-node x 32) that work on a node.
+#define AMMSB_PHI_REG_SHAPES(X)                                                         \
+  X(1, 1, 1) X(2, 1, 1) X(4, 1, 1) X(8, 1, 1) X(16, 1, 1) X(32, 1, 1) X(32, 1, 2)       \
+  X(32, 1, 4) X(32, 2, 1) X(32, 2, 2) X(32, 2, 4) X(32, 4, 1) X(32, 4, 2) X(32, 4, 4)   \
+  X(32, 8, 1) X(32, 8, 2) X(32, 8, 4) X(16, 1, 2) X(8, 1, 2) X(8, 1, 4) X(16, 2, 1)     \
+  X(8, 2, 1) X(8, 4, 1) X(4, 2, 1) X(4, 4, 1)
+
+// Ring depths the bulk-copy update_phi kernel is built for.
+#define AMMSB_PHI_TMA_STAGES(X) X(3) X(4) X(6)
+
+namespace ammsb_detail {
+// Raises a kernel's dynamic shared memory limit to at least `bytes` and
+// never lowers it: the limit belongs to the kernel, not to a handle, and
+// handles of different sizes share kernels.
+template <typename F>
+cudaError_t raise_smem_limit(F* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> set;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = set[std::make_pair(dev, reinterpret_cast<const void*>(kernel))];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
+// Reads the device error word of a handle (synchronises its stream).
+int check_device_err(ammsb_handle* h);
+// Drops draws made ahead of time and points the next draw at step_count.
+int invalidate_prefetch(ammsb_handle* h);
+}  // namespace ammsb_detail

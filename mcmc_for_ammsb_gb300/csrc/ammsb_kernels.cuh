@@ -58,6 +58,17 @@ struct Buffers {
   DevCounters* gc;     // sampler-wide counters
 };
 
+// One chain of a multi-chain launch (blockIdx.y selects the chain): its
+// model, graph and both buffer sets, plus the per-chain launch parameters
+// of the single-chain kernels.
+struct ChainArgs {
+  Model m;
+  DevGraph g;
+  Buffers b[2];
+  int32_t ncommit;    // k_commit_beta: blocks of the commit part
+  int32_t smem_hash;  // k_sample_minibatch: the dedup hash fits shared memory
+};
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -142,8 +153,8 @@ __device__ __forceinline__ int block_scan_1024(bool flag, int* s_warp, int* tota
 // (atomicMin of its index in a hash), then an ordered block scan appends
 // them -- exactly the sequential scan of the oracle.
 // ---------------------------------------------------------------------------
-static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, Buffers b,
-                                                                  int smem_hash) {
+static __device__ __forceinline__ void sample_minibatch_body(const Model& m, const DevGraph& g,
+                                                             const Buffers& b, int smem_hash) {
   extern __shared__ uint32_t s_htab[];  // dedup hash in shared memory when it fits
   constexpr int kRowCap = 2048;         // the source's row, staged when it fits
   __shared__ int32_t s_row[kRowCap];
@@ -192,26 +203,33 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
     __syncthreads();
     int count = 0;
     uint64_t t = 0;
+    // the spec scans candidates t = 0, 1, ... until mb are kept, giving up
+    // at `cap`; a round examines R >= need of them in parallel and keeps the
+    // first new valid ones, in order, up to mb.  R grows beyond need (up to
+    // one 4096-candidate pass) while the dedup hash stays at most half full,
+    // so small populations with many repeats finish in a round or two.
     const uint64_t cap = 64ull * (uint64_t)mb + 4096ull;
+    const int half = (int)((b.hmask + 1u) / 2u);
     while (!err && count < mb) {
       const int need = mb - count;
-      if (t + (uint64_t)need > cap) {
+      if (t >= cap) {
         err |= kErrMinibatchCap;
         break;
       }
+      const int R = (int)min((uint64_t)max(need, min(half - count, 4096)), cap - t);
       // pass A: validity and first-occurrence index per value.  Thread tid
       // owns the G consecutive candidates c0 + G*tid + j of each chunk of
       // G*blockDim.x; the first exclusion probes of all G are issued together.
       constexpr int G = 4;
       const int chunk = G * (int)blockDim.x;
-      for (int c0 = 0; c0 < need; c0 += chunk) {
+      for (int c0 = 0; c0 < R; c0 += chunk) {
         int32_t u[G];
         bool live[G];
         unsigned long long key[G], xs[G], xk[G];
 #pragma unroll
         for (int j = 0; j < G; ++j) {
           const int c = c0 + G * tid + j;
-          live[j] = c < need;
+          live[j] = c < R;
           u[j] = live[j] ? (int32_t)uniform_below(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c),
                                                   (uint64_t)g.n)
                          : -1;
@@ -224,7 +242,7 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
 #pragma unroll
         for (int j = 0; j < G; ++j) {
           const int c = c0 + G * tid + j;
-          if (c >= need) continue;
+          if (c >= R) continue;
           const bool linked = live[j] && (row_in_smem ? row_contains(s_row, vdeg, u[j])
                                                       : has_edge(g, v, u[j]));
           const bool ok = live[j] && !linked &&
@@ -245,8 +263,9 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
       }
       __syncthreads();
       // pass B: ordered compaction of first occurrences, one block scan per
-      // chunk (thread-local counts of G consecutive candidates)
-      for (int c0 = 0; c0 < need; c0 += chunk) {
+      // chunk (thread-local counts of G consecutive candidates); count is
+      // block-uniform, so every thread leaves the loop together at mb
+      for (int c0 = 0; c0 < R && count < mb; c0 += chunk) {
         int32_t u[G];
         bool acc[G];
         int mine = 0;
@@ -255,7 +274,7 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
           const int c = c0 + G * tid + j;
           u[j] = -1;
           acc[j] = false;
-          if (c < need) {
+          if (c < R) {
             u[j] = b.cand[c];
             if (u[j] >= 0) {
               uint32_t slot = hash32((uint32_t)u[j]) & b.hmask;
@@ -278,16 +297,18 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
         for (int j = 0; j < G; ++j) {
           if (acc[j]) {
             const int e = count + pos;
-            b.nodes[e + 1] = u[j];
-            b.ea[e] = 0;
-            b.eb[e] = e + 1;
-            b.ey[e] = 0;
+            if (e < mb) {
+              b.nodes[e + 1] = u[j];
+              b.ea[e] = 0;
+              b.eb[e] = e + 1;
+              b.ey[e] = 0;
+            }
             ++pos;
           }
         }
-        count += total;
+        count = min(count + total, mb);
       }
-      t += (uint64_t)need;
+      t += (uint64_t)R;
       ++rounds;
       __syncthreads();
     }
@@ -342,6 +363,16 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
     if (err) atomicOr(&b.gc->err, err);
   }
 }
+static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGraph g, Buffers b,
+                                                                  int smem_hash) {
+  sample_minibatch_body(m, g, b, smem_hash);
+}
+// one CTA per chain (blockIdx.y), buffer set p
+static __global__ void __launch_bounds__(1024) k_sample_minibatch_chains(const ChainArgs* __restrict__ c,
+                                                                         int p) {
+  const ChainArgs& a = c[blockIdx.y];
+  sample_minibatch_body(a.m, a.g, a.b[p], a.smem_hash);
+}
 
 // ---------------------------------------------------------------------------
 // k_sample_neighbors: one warp per minibatch node.  n_out distinct ids j,
@@ -350,7 +381,7 @@ static __global__ void __launch_bounds__(1024) k_sample_minibatch(Model m, DevGr
 // graph membership the update needs (cc:279-283).
 // ---------------------------------------------------------------------------
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGraph g, Buffers b) {
+__device__ __forceinline__ void sample_neighbors_body(const Model& m, const DevGraph& g, const Buffers& b) {
   // per warp: a set of the ids accepted so far (open addressing, capacity a
   // power of two >= 2 n_out, -1 empty) in dynamic shared memory
   extern __shared__ int32_t s_sets[];
@@ -421,6 +452,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
     __syncwarp();  // srow and set are reused by the warp's next node
   }
 }
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGraph g, Buffers b) {
+  sample_neighbors_body<WARPS>(m, g, b);
+}
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors_chains(const ChainArgs* __restrict__ c,
+                                                                      int p) {
+  const ChainArgs& a = c[blockIdx.y];
+  sample_neighbors_body<WARPS>(a.m, a.g, a.b[p]);
+}
 
 // ---------------------------------------------------------------------------
 // k_update_phi: update_phi (cc:269-313) for NPB minibatch nodes per CTA,
@@ -442,8 +483,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_sample_neighbors(Model m, DevGra
 // buffer (pi itself is written after all nodes, by k_commit_beta).
 // ---------------------------------------------------------------------------
 template <typename PiT, int LPN, int VPL, int SPLIT, int NPB>
-__global__ void __launch_bounds__(NPB * SPLIT * LPN)
-    k_update_phi(Model m, Buffers b) {
+__device__ __forceinline__ void update_phi_body(const Model& m, const Buffers& b) {
   using TR = PiTraits<PiT>;
   constexpr int EV = TR::kPerVec;
   constexpr int EPL = VPL * EV;
@@ -627,6 +667,16 @@ __global__ void __launch_bounds__(NPB * SPLIT * LPN)
     __syncthreads();
   }
 }
+template <typename PiT, int LPN, int VPL, int SPLIT, int NPB>
+__global__ void __launch_bounds__(NPB * SPLIT * LPN) k_update_phi(Model m, Buffers b) {
+  update_phi_body<PiT, LPN, VPL, SPLIT, NPB>(m, b);
+}
+template <typename PiT, int LPN, int VPL, int SPLIT, int NPB>
+__global__ void __launch_bounds__(NPB * SPLIT * LPN) k_update_phi_chains(const ChainArgs* __restrict__ c,
+                                                                         int p) {
+  const ChainArgs& a = c[blockIdx.y];
+  update_phi_body<PiT, LPN, VPL, SPLIT, NPB>(a.m, a.b[p]);
+}
 
 // ---------------------------------------------------------------------------
 // k_commit_beta: blocks [0, ncommit) copy the staged rows into pi (the
@@ -638,7 +688,7 @@ __global__ void __launch_bounds__(NPB * SPLIT * LPN)
 // theta factors), accumulated per warp in registers, then per block.
 // ---------------------------------------------------------------------------
 template <typename PiT, int KQ>
-__global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int ncommit) {
+__device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& b, int ncommit) {
   using TR = PiTraits<PiT>;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Kp = m.Kp, K = m.K;
@@ -663,7 +713,7 @@ __global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int nco
   __shared__ float s_part[4][2][KQ * 128];
   const int bb = blockIdx.x - ncommit;
   const int n_edges = b.st->n_edges;
-  if (bb * 4 >= n_edges) return;  // no edges for this block: k_theta skips its partial
+  if (bb >= m.nbb || bb * 4 >= n_edges) return;  // no edges for this block: k_theta skips its partial
   float R0[KQ * 4], R1[KQ * 4], bt[KQ * 4];
 #pragma unroll
   for (int q = 0; q < KQ; ++q)
@@ -728,6 +778,15 @@ __global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int nco
     out[Kp + k] = s_part[0][1][k] + s_part[1][1][k] + s_part[2][1][k] + s_part[3][1][k];
   }
 }
+template <typename PiT, int KQ>
+__global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int ncommit) {
+  commit_beta_body<PiT, KQ>(m, b, ncommit);
+}
+template <typename PiT, int KQ>
+__global__ void __launch_bounds__(128) k_commit_beta_chains(const ChainArgs* __restrict__ c, int p) {
+  const ChainArgs& a = c[blockIdx.y];
+  commit_beta_body<PiT, KQ>(a.m, a.b[p], a.ncommit);
+}
 
 // ---------------------------------------------------------------------------
 // k_theta: theta step of update_beta (cc:241-266) in FP64.  With the block
@@ -735,7 +794,7 @@ __global__ void __launch_bounds__(128) k_commit_beta(Model m, Buffers b, int nco
 //   G_k0 = beta R1 (0 - 1/ts) + (1-beta) R0 (1/theta_k0 - 1/ts)
 //   G_k1 = beta R1 (1/theta_k1 - 1/ts) + (1-beta) R0 (0 - 1/ts)
 // ---------------------------------------------------------------------------
-static __global__ void __launch_bounds__(1024) k_theta(Model m, Buffers b) {
+static __device__ __forceinline__ void theta_body(const Model& m, const Buffers& b) {
   // 32 consecutive k per CTA; warp w sums the partials of the active beta
   // blocks w, w+32, ... in FP32 with Kahan compensation, then warp 0 adds
   // the 32 warp sums in fixed order (deterministic) and takes the FP64 step.
@@ -802,6 +861,11 @@ static __global__ void __launch_bounds__(1024) k_theta(Model m, Buffers b) {
   b.theta[2 * k] = t0;
   b.theta[2 * k + 1] = t1;
   b.beta[k] = (float)(t1 / (t0 + t1));
+}
+static __global__ void __launch_bounds__(1024) k_theta(Model m, Buffers b) { theta_body(m, b); }
+static __global__ void __launch_bounds__(1024) k_theta_chains(const ChainArgs* __restrict__ c, int p) {
+  const ChainArgs& a = c[blockIdx.y];
+  theta_body(a.m, a.b[p]);
 }
 
 // ---------------------------------------------------------------------------

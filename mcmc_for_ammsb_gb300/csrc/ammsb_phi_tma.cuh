@@ -172,7 +172,7 @@ __device__ __forceinline__ void load_row_pairs(const PiT* row, int lane, int nve
 // every node), refilling each slot, branch-free, with the row STAGES ahead
 // as soon as the row in it is consumed.
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
-__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1) k_update_phi_tma(Model m, Buffers b) {
+__device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffers& b) {
   using TR = PiTraits<PiT>;
   constexpr int EV = TR::kPerVec;
   constexpr int EPL = VPL * EV;
@@ -419,6 +419,16 @@ __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 
     }
     __syncthreads();  // smem reuse by the next node
   }
+}
+template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
+__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1) k_update_phi_tma(Model m, Buffers b) {
+  update_phi_tma_body<PiT, VPL, SPLIT, STAGES, FULL>(m, b);
+}
+template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
+__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1)
+    k_update_phi_tma_chains(const ChainArgs* __restrict__ c, int p) {
+  const ChainArgs& a = c[blockIdx.y];
+  update_phi_tma_body<PiT, VPL, SPLIT, STAGES, FULL>(a.m, a.b[p]);
 }
 
 }  // namespace ammsb

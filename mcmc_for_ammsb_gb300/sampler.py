@@ -80,6 +80,20 @@ class MCMCSamplerStochastic:
             self._h, phi.ctypes.data_as(_native._F32P), theta.ctypes.data_as(_native._F64P)))
         return self
 
+    def autotune(self, reps=5, fresh=False):
+        """Times the built update_phi shapes for this chain (ammsb_autotune)
+        and keeps the fastest; returns the configuration in use."""
+        self._check(_native.lib().ammsb_autotune(self._h, int(reps),
+                                                 _native.TUNE_FRESH if fresh else 0))
+        return self.kernel_config()
+
+    def kernel_config(self):
+        """(bulk-copy kernel, lanes per node, vectors per lane, sub-groups
+        per node, ring depth) of update_phi."""
+        out = (ctypes.c_int32 * 5)()
+        self._check(_native.lib().ammsb_get_kernel_config(self._h, out))
+        return dict(zip(("tma", "lanes", "vectors", "split", "stages"), list(out)))
+
     def save_checkpoint(self, path):
         """Writes the whole chain (state, counters, running averages, Philox
         key) to `path`; see ammsb_save_checkpoint."""
@@ -230,3 +244,45 @@ class MCMCSamplerStochastic:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class ChainBatch:
+    """Independent chains advanced together, one CUDA graph launch per
+    iteration for all of them (ammsb_batch_*).  Every sampler keeps its own
+    graph, state and step counter; step(n) advances all of them by n."""
+
+    def __init__(self, samplers):
+        self.samplers = list(samplers)
+        if not self.samplers:
+            raise ValueError("need at least one sampler")
+        for s in self.samplers:
+            s.create()
+        arr = (ctypes.c_void_p * len(self.samplers))(*[s._h.value for s in self.samplers])
+        out = ctypes.c_void_p()
+        code = _native.lib().ammsb_batch_create(arr, len(self.samplers), ctypes.byref(out))
+        if code != _native.AMMSB_OK:
+            raise _native.AmmsbError(code, (_native.lib().ammsb_batch_create_error() or b"").decode())
+        self._b = out
+
+    def step(self, n=1):
+        code = _native.lib().ammsb_batch_step(self._b, int(n))
+        if code != _native.AMMSB_OK:
+            raise _native.AmmsbError(code, (_native.lib().ammsb_batch_last_error(self._b) or b"").decode())
+
+    def groups(self):
+        """update_phi launches per iteration (distinct kernel shapes)."""
+        return _native.lib().ammsb_batch_groups(self._b)
+
+    def stream(self):
+        return _native.lib().ammsb_batch_stream(self._b)
+
+    def close(self):
+        if getattr(self, "_b", None) is not None:
+            _native.lib().ammsb_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

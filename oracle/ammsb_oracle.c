@@ -198,29 +198,26 @@ static int sample_nonlinks(const oracle_graph *g, int64_t m, uint32_t seed,
   nodes[0] = v;
   int32_t count = 0;
   int64_t t = 0;
-  int32_t rounds = 0;
+  /* candidates t = 0, 1, ... in draw order; the first m valid, new ones are
+   * kept; the scan gives up when NONLINK_CAND_CAP(m) candidates are used */
   while (count < m) {
-    int64_t need = m - count;
-    if (t + need > NONLINK_CAND_CAP(m)) return -1;
-    for (int64_t c = 0; c < need; ++c) {
-      int32_t u = (int32_t)below(oracle_draw_u64(seed, chain, OR_P_MB_CAND, 0, step,
-                                                 (uint64_t)(t + c)),
-                                 (uint64_t)N);
-      if (u == v) continue;
-      if (oracle_has_edge(g, v, u) || oracle_is_excluded(g, v, u)) continue;
-      if (in_list(nodes + 1, count, u)) continue;
-      nodes[count + 1] = u;
-      ea[count] = 0;
-      eb[count] = count + 1;
-      ey[count] = 0;
-      count++;
-    }
-    t += need;
-    rounds++;
+    if (t >= NONLINK_CAND_CAP(m)) return -1;
+    int32_t u = (int32_t)below(oracle_draw_u64(seed, chain, OR_P_MB_CAND, 0, step,
+                                               (uint64_t)t),
+                               (uint64_t)N);
+    t++;
+    if (u == v) continue;
+    if (oracle_has_edge(g, v, u) || oracle_is_excluded(g, v, u)) continue;
+    if (in_list(nodes + 1, count, u)) continue;
+    nodes[count + 1] = u;
+    ea[count] = 0;
+    eb[count] = count + 1;
+    ey[count] = 0;
+    count++;
   }
   info->n_edges = count;
   info->n_nodes = count + 1;
-  info->rounds = rounds;
+  info->rounds = (int32_t)(t < 0x7fffffff ? t : 0x7fffffff); /* candidates used */
   return 0;
 }
 
