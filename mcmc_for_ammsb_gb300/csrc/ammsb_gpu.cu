@@ -350,10 +350,8 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
     return fail("graph: need 2 <= n <= 2^31-1 and CSR arrays", AMMSB_E_ARG);
   if (o.K < 1 || o.K > 1024) return fail("K must be in [1, 1024]", AMMSB_E_ARG);
   if (o.strategy < 0 || o.strategy > 3) return fail("Invalid sampling strategy", AMMSB_E_ARG);
-  if (o.strategy == AMMSB_RANDOM_EDGE)
-    return fail("strategy random-edge is not implemented on the GPU path", AMMSB_E_UNSUPPORTED);
-  if (o.sampler_max_source != 1)
-    return fail("sampler.max-source > 1 is not implemented on the GPU path", AMMSB_E_UNSUPPORTED);
+  if (o.sampler_max_source < 1 || o.sampler_max_source > 2048)
+    return fail("sampler.max-source must be in [1, 2048]", AMMSB_E_ARG);
   if (o.pi_dtype != AMMSB_PI_F32 && o.pi_dtype != AMMSB_PI_BF16)
     return fail("pi_dtype must be AMMSB_PI_F32 or AMMSB_PI_BF16", AMMSB_E_ARG);
   // derived defaults: options.h:257-262, learner.cc:88-92, cc:15-24, 35-44
@@ -366,8 +364,9 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   if (o.mini_batch_size == 0) o.mini_batch_size = N / 10;
   if (o.num_node_sample < 1 || o.num_node_sample + 1 > N - 1)
     return fail("num_node_sample must be in [1, N-2]", AMMSB_E_ARG);
-  if (o.mini_batch_size < 1 || o.mini_batch_size > N - 1 || o.mini_batch_size > (1 << 24))
-    return fail("mini_batch_size must be in [1, min(N-1, 2^24)]", AMMSB_E_ARG);
+  if (o.mini_batch_size < 1 || o.mini_batch_size > (1 << 24) ||
+      (o.strategy != AMMSB_RANDOM_EDGE && o.mini_batch_size > N - 1))
+    return fail("mini_batch_size must be in [1, 2^24] (and <= N-1 for node strategies)", AMMSB_E_ARG);
   if (o.b <= 0 || o.epsilon <= 0 || o.epsilon >= 1) return fail("invalid b or epsilon", AMMSB_E_ARG);
 
   // validate the CSR: monotone row_ptr, ids in range, sorted rows, no self loops
@@ -434,9 +433,29 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   m.seed = (uint32_t)o.random_seed;
   m.chain = (uint32_t)o.chain;
   m.n_out = (int32_t)o.num_node_sample + 1;
-  const int64_t max_edges = std::max<int64_t>(o.mini_batch_size, std::max<int64_t>(maxdeg, 1));
+  // minibatch capacities (network.cc:172-201): one source's star for the
+  // stratified strategies; m + max degree with several link sources; m
+  // edges for random-edge, or the whole training set when m reaches it
+  // (E - |held-out| - |test|, network.cc:238-241)
+  const bool multi_src = o.sampler_max_source > 1;
+  const bool rand_edge = o.strategy == AMMSB_RANDOM_EDGE;
+  m.full_set = (rand_edge && o.mini_batch_size >= h->E - h->H - h->T) ? 1 : 0;
+  int64_t max_edges = std::max<int64_t>(o.mini_batch_size, std::max<int64_t>(maxdeg, 1));
+  if (multi_src) max_edges = o.mini_batch_size + std::max<int64_t>(maxdeg, 1);
+  if (rand_edge) max_edges = m.full_set ? std::max<int64_t>(h->E, 1) : o.mini_batch_size;
+  if (max_edges > (1 << 28)) {
+    h->err = "minibatch capacity too large";
+    return bail(AMMSB_E_CAPACITY);
+  }
+  if (rand_edge && nnz >= (int64_t)INT32_MAX) {
+    h->err = "random-edge needs fewer than 2^30 edges";
+    return bail(AMMSB_E_UNSUPPORTED);
+  }
   m.max_edges = (int32_t)max_edges;
-  m.max_nodes = (int32_t)(max_edges + 1);
+  m.max_nodes = (multi_src || rand_edge) ? (int32_t)std::min<int64_t>(N, 2 * max_edges + 1)
+                                         : (int32_t)(max_edges + 1);
+  m.max_source = (int32_t)o.sampler_max_source;
+  m.n_entries = nnz;
   m.mini_batch_size = (int32_t)o.mini_batch_size;
   m.strategy = o.strategy;
   {  // network.cc:341-342 with Float = float
@@ -545,7 +564,11 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   // a minibatch round examines up to max(remaining, 4096) candidates while
   // the dedup hash stays at most half full
   TRY(dev_alloc(h, &b.cand, (size_t)std::max<int64_t>(o.mini_batch_size, 4096)));
-  const int hcap = next_pow2(std::max<int64_t>(8192, 2 * o.mini_batch_size));
+  // ... and numbers the nodes of a general edge list (random-edge, several
+  // link sources) in the same table: at most max_nodes distinct vertices
+  int64_t hneed = std::max<int64_t>(8192, 2 * o.mini_batch_size);
+  if (multi_src || rand_edge) hneed = std::max<int64_t>(hneed, 2 * (int64_t)m.max_nodes);
+  const int hcap = next_pow2(hneed);
   TRY(dev_alloc(h, &b.htab_key, (size_t)hcap));
   TRY(dev_alloc(h, &b.htab_idx, (size_t)hcap));
   b.hmask = (uint32_t)(hcap - 1);

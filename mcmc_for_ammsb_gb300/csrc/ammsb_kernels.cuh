@@ -34,6 +34,9 @@ struct Model {
   float nonlink_scale, link_scale;
   int32_t nbb;    // beta partial blocks
   int32_t nbr_set_cap;  // per-warp accepted-neighbour set capacity (power of two)
+  int32_t max_source;   // sampler.max-source (link stratum)
+  int32_t full_set;     // random-edge: the minibatch is the whole training set
+  int64_t n_entries;    // 2E: entries of the symmetric CSR
 };
 
 struct Buffers {
@@ -142,6 +145,101 @@ __device__ __forceinline__ int block_scan_1024(bool flag, int* s_warp, int* tota
   return pos;
 }
 
+// Open-addressing insert of key into (hkey, hidx): keeps the smallest
+// position per key.  The table is never full (callers keep it at most half
+// full), so the probe ends.
+__device__ __forceinline__ void hash_insert_min(uint32_t* hkey, uint32_t* hidx, uint32_t hmask,
+                                                uint32_t key, uint32_t pos) {
+  uint32_t slot = hash32(key) & hmask;
+  for (uint32_t probe = 0; probe <= hmask; ++probe) {
+    const uint32_t prev = atomicCAS(hkey + slot, 0xffffffffu, key);
+    if (prev == 0xffffffffu || prev == key) {
+      atomicMin(hidx + slot, pos);
+      return;
+    }
+    slot = (slot + 1) & hmask;
+  }
+}
+
+// Value stored for key (0xffffffff when absent).
+__device__ __forceinline__ uint32_t hash_find(const uint32_t* hkey, const uint32_t* hidx,
+                                              uint32_t hmask, uint32_t key) {
+  uint32_t slot = hash32(key) & hmask;
+  for (uint32_t probe = 0; probe <= hmask; ++probe) {
+    const uint32_t k = hkey[slot];
+    if (k == key) return hidx[slot];
+    if (k == 0xffffffffu) return 0xffffffffu;
+    slot = (slot + 1) & hmask;
+  }
+  return 0xffffffffu;
+}
+
+// Row of entry q of the CSR: the last v with row_ptr[v] <= q.
+__device__ __forceinline__ int32_t csr_row_of(const int64_t* row_ptr, int64_t n, int64_t q) {
+  int64_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (__ldg(row_ptr + mid) <= q) lo = mid; else hi = mid;
+  }
+  return (int32_t)lo;
+}
+
+// Node numbering of a general edge list: ea/eb hold the vertex ids of
+// `count` edges; the nodes are numbered by first appearance over (a0, b0,
+// a1, b1, ...), written to nodes[], and ea/eb are rewritten as slots.
+// Returns the node count (or -1 past max_nodes).  Block-wide; uses the
+// dedup hash (reset here) and s_warp.
+static __device__ int assign_node_slots(const Buffers& b, int count, int max_nodes, uint32_t* hkey,
+                                 uint32_t* hidx, int* s_warp) {
+  const int tid = threadIdx.x;
+  for (uint32_t s = tid; s <= b.hmask; s += blockDim.x) {
+    hkey[s] = 0xffffffffu;
+    hidx[s] = 0xffffffffu;
+  }
+  __syncthreads();
+  const int np = 2 * count;
+  for (int p = tid; p < np; p += blockDim.x) {
+    const uint32_t x = (uint32_t)((p & 1) ? b.eb[p >> 1] : b.ea[p >> 1]);
+    hash_insert_min(hkey, hidx, b.hmask, x, (uint32_t)p);
+  }
+  __syncthreads();
+  int n = 0;
+  for (int base = 0; base < np; base += blockDim.x) {
+    const int p = base + tid;
+    bool first = false;
+    uint32_t x = 0;
+    if (p < np) {
+      x = (uint32_t)((p & 1) ? b.eb[p >> 1] : b.ea[p >> 1]);
+      first = hash_find(hkey, hidx, b.hmask, x) == (uint32_t)p;
+    }
+    int total;
+    const int pos = block_scan_1024(first, s_warp, &total);
+    if (first && n + pos < max_nodes) b.nodes[n + pos] = (int32_t)x;
+    n += total;
+  }
+  if (n > max_nodes) return -1;
+  __syncthreads();
+  // the hash now maps vertex -> slot
+  for (int s = tid; s < n; s += blockDim.x) {
+    const uint32_t x = (uint32_t)b.nodes[s];
+    uint32_t slot = hash32(x) & b.hmask;
+    for (uint32_t probe = 0; probe <= b.hmask; ++probe) {
+      if (hkey[slot] == x) {
+        hidx[slot] = (uint32_t)s;
+        break;
+      }
+      slot = (slot + 1) & b.hmask;
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < count; e += blockDim.x) {
+    b.ea[e] = (int32_t)hash_find(hkey, hidx, b.hmask, (uint32_t)b.ea[e]);
+    b.eb[e] = (int32_t)hash_find(hkey, hidx, b.hmask, (uint32_t)b.eb[e]);
+  }
+  __syncthreads();
+  return n;
+}
+
 // ---------------------------------------------------------------------------
 // k_sample_minibatch: one 1024-thread CTA.  Stratified random node
 // (network.cc:410-421): flag = randint(0,1); non-link stratum
@@ -159,8 +257,10 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
   constexpr int kRowCap = 2048;         // the source's row, staged when it fits
   __shared__ int32_t s_row[kRowCap];
   __shared__ int s_warp[33];
-  __shared__ int s_flag, s_count;
+  __shared__ int s_flag, s_count, s_nodes;
   __shared__ uint32_t s_step;
+  __shared__ int32_t s_v;
+  __shared__ int s_brk, s_dup;
   const int tid = threadIdx.x;
   const Stream rs{m.seed, m.chain};
   if (tid == 0) {
@@ -170,11 +270,14 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
     int flag;
     if (m.strategy == 0)
       flag = (int)uniform_below(rs.draw_u64(kTagMbFlag, 0, step, 0), 2ull);
+    else if (m.strategy == 3)
+      flag = 2;  // random-edge
     else
       flag = (m.strategy == 1) ? 1 : 0;
     s_flag = flag;
     s_step = step;
     s_count = 0;
+    s_nodes = 0;
   }
   __syncthreads();
   const uint32_t step = s_step;
@@ -315,6 +418,161 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
     if (tid == 0) {
       b.st->scale = m.nonlink_scale;
       s_count = count;
+      s_nodes = count + 1;
+    }
+  } else if (flag == 2) {
+    // random_edge_sampling (network.cc:237-268): m distinct training edges,
+    // candidates = entries of the symmetric CSR (each edge twice, as the
+    // reference's linked_edges), kept when a < b and not held-out/test; the
+    // whole training set when m reaches it (network.cc:215-234)
+    const int mb = m.mini_batch_size;
+    uint32_t* hkey = smem_hash ? s_htab : b.htab_key;
+    uint32_t* hidx = smem_hash ? s_htab + (b.hmask + 1) : b.htab_idx;
+    int count = 0;
+    if (m.full_set) {
+      for (int64_t base = 0; base < m.n_entries && !err; base += blockDim.x) {
+        const int64_t q = base + tid;
+        bool acc = false;
+        int32_t a = 0, c = 0;
+        if (q < m.n_entries) {
+          a = csr_row_of(g.row_ptr, g.n, q);
+          c = g.col[q];
+          acc = a < c && !is_excluded(g, a, c);
+        }
+        int total;
+        const int pos = block_scan_1024(acc, s_warp, &total);
+        if (acc && count + pos < m.max_edges) {
+          b.ea[count + pos] = a;
+          b.eb[count + pos] = c;
+          b.ey[count + pos] = 1;
+        }
+        count += total;
+        if (count > m.max_edges) err |= kErrCapacity;
+      }
+    } else {
+      for (uint32_t sl = tid; sl <= b.hmask; sl += blockDim.x) {
+        hkey[sl] = 0xffffffffu;
+        hidx[sl] = 0xffffffffu;
+      }
+      if (mb > m.max_edges) err |= kErrCapacity;
+      __syncthreads();
+      uint64_t t = 0;
+      const uint64_t cap = 64ull * (uint64_t)mb + 4096ull;
+      const int half = (int)((b.hmask + 1u) / 2u);
+      while (!err && count < mb) {
+        const int need = mb - count;
+        if (t >= cap) {
+          err |= kErrMinibatchCap;
+          break;
+        }
+        const int R = (int)min((uint64_t)max(need, min(half - count, 4096)), cap - t);
+        for (int c = tid; c < R; c += blockDim.x) {
+          const int64_t q = (int64_t)uniform_below(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c),
+                                                   (uint64_t)m.n_entries);
+          const int32_t a = csr_row_of(g.row_ptr, g.n, q), bb = g.col[q];
+          const bool ok = a < bb && !is_excluded(g, a, bb);
+          b.cand[c] = ok ? (int32_t)q : -1;
+          if (ok) hash_insert_min(hkey, hidx, b.hmask, (uint32_t)q, (uint32_t)(t + (uint64_t)c));
+        }
+        __syncthreads();
+        for (int base = 0; base < R && count < mb; base += blockDim.x) {
+          const int c = base + tid;
+          int32_t q = -1;
+          bool acc = false;
+          if (c < R) {
+            q = b.cand[c];
+            acc = q >= 0 && hash_find(hkey, hidx, b.hmask, (uint32_t)q) == (uint32_t)(t + (uint64_t)c);
+          }
+          int total;
+          const int pos = block_scan_1024(acc, s_warp, &total);
+          if (acc && count + pos < mb) {
+            b.ea[count + pos] = csr_row_of(g.row_ptr, g.n, q);
+            b.eb[count + pos] = g.col[q];
+            b.ey[count + pos] = 1;
+          }
+          count = min(count + total, mb);
+        }
+        t += (uint64_t)R;
+        ++rounds;
+        __syncthreads();
+      }
+    }
+    int n = 0;
+    if (!err) {
+      n = assign_node_slots(b, count, m.max_nodes, hkey, hidx, s_warp);
+      if (n < 0) err |= kErrCapacity;
+    }
+    if (tid == 0) {
+      b.st->scale = count > 0 ? (float)((double)(m.N - 1) * (double)m.N / 2.0 / (double)count) : 0.f;
+      s_count = count;
+      s_nodes = n;
+    }
+  } else if (m.max_source > 1) {
+    // stratified_random_node_sampling_links with sampler.max-source > 1
+    // (network.cc:355-407): up to S sources per attempt (draw a*S + s); from
+    // the second on, one whose degree would pass m ends the attempt; each
+    // source adds its training edges once (an edge to an earlier source was
+    // added from it; a repeated source adds none); redrawn while empty
+    const int mb = m.mini_batch_size, S = m.max_source;
+    uint32_t* hkey = smem_hash ? s_htab : b.htab_key;
+    uint32_t* hidx = smem_hash ? s_htab + (b.hmask + 1) : b.htab_idx;
+    int32_t* s_src = s_row;  // the attempt's sources (S <= kRowCap)
+    int count = 0;
+    for (int attempt = 0; attempt < 4096 && count == 0 && !err; ++attempt) {
+      count = 0;
+      for (int sidx = 0; sidx < S && !err; ++sidx) {
+        if (tid == 0) {
+          const int32_t v = (int32_t)uniform_below(
+              rs.draw_u64(kTagMbNode, 0, step, (uint64_t)attempt * (uint64_t)S + (uint64_t)sidx),
+              (uint64_t)g.n);
+          const int64_t deg = g.row_ptr[v + 1] - g.row_ptr[v];
+          int dup = 0;
+          for (int r = 0; r < sidx; ++r) dup |= (s_src[r] == v);
+          s_brk = (sidx > 0 && (int64_t)count + deg > (int64_t)mb) ? 1 : 0;
+          s_dup = dup;
+          s_v = v;
+          if (!s_brk) s_src[sidx] = v;
+        }
+        __syncthreads();
+        const int32_t v = s_v;
+        const int brk = s_brk, dup = s_dup;
+        __syncthreads();
+        if (brk) break;
+        if (dup) continue;
+        const int64_t r0 = g.row_ptr[v];
+        const int deg = (int)(g.row_ptr[v + 1] - r0);
+        for (int base = 0; base < deg; base += blockDim.x) {
+          const int q = base + tid;
+          int32_t u = -1;
+          bool acc = false;
+          if (q < deg) {
+            u = g.col[r0 + q];
+            acc = !is_excluded(g, v, u);
+            for (int r = 0; r < sidx && acc; ++r) acc = (s_src[r] != u);
+          }
+          int total;
+          const int pos = block_scan_1024(acc, s_warp, &total);
+          if (acc && count + pos < m.max_edges) {
+            b.ea[count + pos] = v;
+            b.eb[count + pos] = u;
+            b.ey[count + pos] = 1;
+          }
+          count += total;
+          if (count > m.max_edges) err |= kErrCapacity;
+        }
+      }
+      rounds = attempt + 1;
+    }
+    if (count == 0 && !err) err |= kErrMinibatchCap;
+    int n = 0;
+    if (!err) {
+      n = assign_node_slots(b, count, m.max_nodes, hkey, hidx, s_warp);
+      if (n < 0) err |= kErrCapacity;
+    }
+    if (tid == 0) {
+      b.st->scale = count > 0 ? (float)(m.n_entries / 2) / (float)count : 0.f;
+      s_count = count;
+      s_nodes = n;
     }
   } else {
     int count = 0;
@@ -352,13 +610,14 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
     if (tid == 0) {
       b.st->scale = m.link_scale;
       s_count = count;
+      s_nodes = count + 1;
     }
   }
   __syncthreads();
   if (tid == 0) {
     b.st->flag = flag;
-    b.st->n_edges = s_count;
-    b.st->n_nodes = err ? 0 : s_count + 1;
+    b.st->n_edges = err ? 0 : s_count;
+    b.st->n_nodes = err ? 0 : s_nodes;
     b.st->rounds = rounds;
     if (err) atomicOr(&b.gc->err, err);
   }

@@ -255,13 +255,152 @@ static int sample_links(const oracle_graph *g, uint32_t seed, uint32_t chain,
   return -1;
 }
 
-int oracle_sample_minibatch(const oracle_graph *g, int strategy,
-                            int64_t mini_batch_size, int64_t num_total_edges,
-                            uint32_t seed, uint32_t chain, uint32_t step,
-                            int32_t *edge_a, int32_t *edge_b, uint8_t *edge_y,
-                            int32_t max_edges, int32_t *nodes,
-                            int32_t max_nodes, oracle_mb_info *info) {
+/* Slot of vertex x among nodes[0 .. *n), appended when new (first
+ * appearance order); -1 when nodes[] is full. */
+static int32_t node_slot(int32_t *nodes, int32_t *n, int32_t max_nodes,
+                         int32_t x) {
+  for (int32_t i = 0; i < *n; ++i)
+    if (nodes[i] == x) return i;
+  if (*n >= max_nodes) return -1;
+  nodes[*n] = x;
+  return (*n)++;
+}
+
+/* stratified_random_node_sampling_links with sampler.max-source = S > 1,
+ * network.cc:355-407: up to S random sources per attempt; from the second
+ * on, a source whose degree would take the set past m ends the attempt;
+ * the training edges of each source are added once each (an edge between
+ * two sources is kept from the earlier one; a repeated source adds
+ * nothing); redrawn while empty.  Source s of attempt a is draw a*S + s.
+ * Nodes are numbered by first appearance, source before partner, so S = 1
+ * gives the layout of sample_links.  scale = num_total_edges / |set|. */
+static int sample_links_multi(const oracle_graph *g, int64_t m, int64_t S,
+                              int64_t num_total_edges, uint32_t seed,
+                              uint32_t chain, uint32_t step, int32_t *ea,
+                              int32_t *eb, uint8_t *ey, int32_t max_edges,
+                              int32_t *nodes, int32_t max_nodes,
+                              oracle_mb_info *info) {
+  int64_t N = g->n;
+  int32_t *srcs = (int32_t *)malloc(sizeof(int32_t) * (size_t)S);
+  for (int32_t attempt = 0; attempt < LINK_ATTEMPT_CAP; ++attempt) {
+    int32_t count = 0, n_nodes = 0;
+    for (int64_t s = 0; s < S; ++s) {
+      int32_t v = (int32_t)below(oracle_draw_u64(seed, chain, OR_P_MB_NODE, 0, step,
+                                                 (uint64_t)attempt * (uint64_t)S + (uint64_t)s),
+                                 (uint64_t)N);
+      int64_t deg = g->row_ptr[v + 1] - g->row_ptr[v];
+      if (s > 0 && count + deg > m) break;
+      int dup = in_list(srcs, (int32_t)s, v);
+      srcs[s] = v;
+      if (dup) continue;
+      for (int64_t p = g->row_ptr[v]; p < g->row_ptr[v + 1]; ++p) {
+        int32_t u = g->col[p];
+        if (oracle_is_excluded(g, v, u)) continue;
+        if (in_list(srcs, (int32_t)s, u)) continue;
+        if (count >= max_edges) { free(srcs); return -2; }
+        int32_t a = node_slot(nodes, &n_nodes, max_nodes, v);
+        int32_t b = node_slot(nodes, &n_nodes, max_nodes, u);
+        if (a < 0 || b < 0) { free(srcs); return -2; }
+        ea[count] = a;
+        eb[count] = b;
+        ey[count] = 1;
+        count++;
+      }
+    }
+    if (count > 0) {
+      free(srcs);
+      info->n_edges = count;
+      info->n_nodes = n_nodes;
+      info->rounds = attempt + 1;
+      info->scale = (float)num_total_edges / (float)count;
+      return 0;
+    }
+  }
+  free(srcs);
+  return -1;
+}
+
+/* random_edge_sampling, network.cc:237-268: m distinct training edges.
+ * Candidates t = 0, 1, ... are entries q of the symmetric CSR (each edge
+ * appears twice, as in the reference's linked_edges), q uniform in [0, 2E);
+ * the entry (a, b) is kept when a < b, (a, b) is neither held-out nor test
+ * and not kept already.  When m >= E - |held-out| - |test| the whole
+ * training set is the minibatch (sample_full_training_set, :215-234), in CSR
+ * order.  Nodes are numbered by first appearance over (a0, b0, a1, b1, ...);
+ * scale = (N - 1) N / 2 / |set| (double, then float). */
+static int sample_random_edge(const oracle_graph *g, int64_t m, uint32_t seed,
+                              uint32_t chain, uint32_t step, int32_t *ea,
+                              int32_t *eb, uint8_t *ey, int32_t max_edges,
+                              int32_t *nodes, int32_t max_nodes,
+                              oracle_mb_info *info) {
+  const int64_t N = g->n, E2 = g->row_ptr[N], E = E2 / 2;
+  int32_t count = 0, n_nodes = 0;
+  if (m >= E - g->n_excl) {
+    for (int32_t a = 0; a < N; ++a)
+      for (int64_t q = g->row_ptr[a]; q < g->row_ptr[a + 1]; ++q) {
+        int32_t b = g->col[q];
+        if (a >= b || oracle_is_excluded(g, a, b)) continue;
+        if (count >= max_edges) return -2;
+        int32_t sa = node_slot(nodes, &n_nodes, max_nodes, a);
+        int32_t sb = node_slot(nodes, &n_nodes, max_nodes, b);
+        if (sa < 0 || sb < 0) return -2;
+        ea[count] = sa;
+        eb[count] = sb;
+        ey[count] = 1;
+        count++;
+      }
+    info->rounds = 0;
+  } else {
+    if (m > max_edges) return -2;
+    int64_t *kept = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m > 0 ? m : 1));
+    int64_t t = 0;
+    while (count < m) {
+      if (t >= NONLINK_CAND_CAP(m)) { free(kept); return -1; }
+      int64_t q = (int64_t)below(oracle_draw_u64(seed, chain, OR_P_MB_CAND, 0, step,
+                                                 (uint64_t)t),
+                                 (uint64_t)E2);
+      t++;
+      int64_t lo = 0, hi = N; /* row of entry q: last a with row_ptr[a] <= q */
+      while (hi - lo > 1) {
+        int64_t mid = (lo + hi) / 2;
+        if (g->row_ptr[mid] <= q) lo = mid; else hi = mid;
+      }
+      int32_t a = (int32_t)lo, b = g->col[q];
+      if (a >= b || oracle_is_excluded(g, a, b)) continue;
+      int seen = 0;
+      for (int32_t i = 0; i < count && !seen; ++i) seen = kept[i] == q;
+      if (seen) continue;
+      int32_t sa = node_slot(nodes, &n_nodes, max_nodes, a);
+      int32_t sb = node_slot(nodes, &n_nodes, max_nodes, b);
+      if (sa < 0 || sb < 0) { free(kept); return -2; }
+      kept[count] = q;
+      ea[count] = sa;
+      eb[count] = sb;
+      ey[count] = 1;
+      count++;
+    }
+    free(kept);
+    info->rounds = (int32_t)(t < 0x7fffffff ? t : 0x7fffffff);
+  }
+  info->n_edges = count;
+  info->n_nodes = n_nodes;
+  info->scale = count > 0 ? (float)((double)(N - 1) * (double)N / 2.0 / (double)count) : 0.0f;
+  return 0;
+}
+
+int oracle_sample_minibatch_ex(const oracle_graph *g, int strategy,
+                               int64_t mini_batch_size, int64_t max_source,
+                               int64_t num_total_edges, uint32_t seed,
+                               uint32_t chain, uint32_t step, int32_t *edge_a,
+                               int32_t *edge_b, uint8_t *edge_y,
+                               int32_t max_edges, int32_t *nodes,
+                               int32_t max_nodes, oracle_mb_info *info) {
   int flag;
+  if (strategy == 3) {
+    info->flag = 2;
+    return sample_random_edge(g, mini_batch_size, seed, chain, step, edge_a,
+                              edge_b, edge_y, max_edges, nodes, max_nodes, info);
+  }
   if (strategy == 0) {
     /* network.cc:410-421: flag = randint(0, 1) */
     flag = (int)below(oracle_draw_u64(seed, chain, OR_P_MB_FLAG, 0, step, 0), 2u);
@@ -278,9 +417,25 @@ int oracle_sample_minibatch(const oracle_graph *g, int strategy,
     return sample_nonlinks(g, mini_batch_size, seed, chain, step, edge_a,
                            edge_b, edge_y, max_edges, nodes, max_nodes, info);
   }
+  if (max_source > 1)
+    return sample_links_multi(g, mini_batch_size, max_source, num_total_edges,
+                              seed, chain, step, edge_a, edge_b, edge_y,
+                              max_edges, nodes, max_nodes, info);
   info->scale = (float)g->n;
   return sample_links(g, seed, chain, step, edge_a, edge_b, edge_y, max_edges,
                       nodes, max_nodes, info);
+}
+
+int oracle_sample_minibatch(const oracle_graph *g, int strategy,
+                            int64_t mini_batch_size, int64_t num_total_edges,
+                            uint32_t seed, uint32_t chain, uint32_t step,
+                            int32_t *edge_a, int32_t *edge_b, uint8_t *edge_y,
+                            int32_t max_edges, int32_t *nodes,
+                            int32_t max_nodes, oracle_mb_info *info) {
+  return oracle_sample_minibatch_ex(g, strategy, mini_batch_size, 1,
+                                    num_total_edges, seed, chain, step, edge_a,
+                                    edge_b, edge_y, max_edges, nodes, max_nodes,
+                                    info);
 }
 
 /* sample_neighbor_nodes, mcmc_sampler_stochastic.h:87-108: n_out distinct
@@ -379,25 +534,34 @@ double oracle_perplexity_f64acc(int32_t K, const float *pi, const int32_t *ha,
 /* ------------------------------------------------------------------------ */
 /* one whole iteration, mcmc_sampler_stochastic.cc:93-183 (loop body)       */
 /* ------------------------------------------------------------------------ */
-int oracle_step_f32(const oracle_params *p, const oracle_graph *g,
-                    uint32_t step, float *pi, float *phi, float *theta,
-                    float *beta, oracle_mb_info *info) {
-  const int32_t K = p->K;
-  int64_t max_edges = p->mini_batch_size;
+/* Edge capacity of one minibatch of the step's strategy (the reference's
+ * max_minibatch_edges_for_strategy, network.cc:188-201, plus the full
+ * training set of random-edge). */
+static int64_t step_max_edges(const oracle_params *p, const oracle_graph *g) {
   int64_t maxdeg = 0;
   for (int64_t v = 0; v < g->n; ++v) {
     int64_t d = g->row_ptr[v + 1] - g->row_ptr[v];
     if (d > maxdeg) maxdeg = d;
   }
-  if (maxdeg > max_edges) max_edges = maxdeg;
+  int64_t me = p->mini_batch_size > maxdeg ? p->mini_batch_size : maxdeg;
+  if (p->max_source > 1) me = p->mini_batch_size + maxdeg;
+  if (p->strategy == 3 && g->row_ptr[g->n] / 2 > me) me = g->row_ptr[g->n] / 2;
+  return me > 0 ? me : 1;
+}
+
+int oracle_step_f32(const oracle_params *p, const oracle_graph *g,
+                    uint32_t step, float *pi, float *phi, float *theta,
+                    float *beta, oracle_mb_info *info) {
+  const int32_t K = p->K;
+  int64_t max_edges = step_max_edges(p, g);
   int32_t *ea = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
   int32_t *eb = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
   uint8_t *ey = (uint8_t *)malloc((size_t)max_edges);
-  int32_t *nodes = (int32_t *)malloc(sizeof(int32_t) * (size_t)(max_edges + 1));
-  int rc = oracle_sample_minibatch(g, p->strategy, p->mini_batch_size,
-                                   p->num_total_edges, p->seed, p->chain, step,
-                                   ea, eb, ey, (int32_t)max_edges, nodes,
-                                   (int32_t)(max_edges + 1), info);
+  int32_t *nodes = (int32_t *)malloc(sizeof(int32_t) * (size_t)(2 * max_edges + 1));
+  int rc = oracle_sample_minibatch_ex(g, p->strategy, p->mini_batch_size,
+                                      p->max_source, p->num_total_edges, p->seed,
+                                      p->chain, step, ea, eb, ey, (int32_t)max_edges,
+                                      nodes, (int32_t)(2 * max_edges + 1), info);
   if (rc != 0) {
     free(ea); free(eb); free(ey); free(nodes);
     return rc;
@@ -463,19 +627,15 @@ int oracle_step_f64(const oracle_params *p, const oracle_graph *g,
                     uint32_t step, double *pi, double *phi, double *theta,
                     double *beta, oracle_mb_info *info) {
   const int32_t K = p->K;
-  int64_t max_edges = p->mini_batch_size;
-  for (int64_t v = 0; v < g->n; ++v) {
-    int64_t d = g->row_ptr[v + 1] - g->row_ptr[v];
-    if (d > max_edges) max_edges = d;
-  }
+  int64_t max_edges = step_max_edges(p, g);
   int32_t *ea = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
   int32_t *eb = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
   uint8_t *ey = (uint8_t *)malloc((size_t)max_edges);
-  int32_t *nodes = (int32_t *)malloc(sizeof(int32_t) * (size_t)(max_edges + 1));
-  int rc = oracle_sample_minibatch(g, p->strategy, p->mini_batch_size,
-                                   p->num_total_edges, p->seed, p->chain, step,
-                                   ea, eb, ey, (int32_t)max_edges, nodes,
-                                   (int32_t)(max_edges + 1), info);
+  int32_t *nodes = (int32_t *)malloc(sizeof(int32_t) * (size_t)(2 * max_edges + 1));
+  int rc = oracle_sample_minibatch_ex(g, p->strategy, p->mini_batch_size,
+                                      p->max_source, p->num_total_edges, p->seed,
+                                      p->chain, step, ea, eb, ey, (int32_t)max_edges,
+                                      nodes, (int32_t)(2 * max_edges + 1), info);
   if (rc != 0) {
     free(ea); free(eb); free(ey); free(nodes);
     return rc;

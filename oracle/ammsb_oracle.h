@@ -93,6 +93,16 @@ int oracle_sample_minibatch(const oracle_graph *g, int strategy,
                             int32_t max_edges, int32_t *nodes,
                             int32_t max_nodes, oracle_mb_info *info);
 
+/* The same with sampler.max-source (network.cc:355-407) for the link
+ * stratum, and strategy 3 = random-edge (network.cc:237-268). */
+int oracle_sample_minibatch_ex(const oracle_graph *g, int strategy,
+                               int64_t mini_batch_size, int64_t max_source,
+                               int64_t num_total_edges, uint32_t seed,
+                               uint32_t chain, uint32_t step, int32_t *edge_a,
+                               int32_t *edge_b, uint8_t *edge_y,
+                               int32_t max_edges, int32_t *nodes,
+                               int32_t max_nodes, oracle_mb_info *info);
+
 /* n_out distinct neighbours of node (n_out = num_node_sample + 1), each
  * != node and not a held-out/test pair; y[t] = graph membership.
  * Returns number of candidate draws used, negative on cap. */
@@ -185,6 +195,7 @@ typedef struct {
   float alpha, epsilon, eta0, eta1;
   double a, b, c;
   uint32_t seed, chain;
+  int64_t max_source; /* sampler.max-source */
 } oracle_params;
 
 /* One SG-MCMC iteration at `step` (draws from the Philox spec), float

@@ -48,7 +48,8 @@ class Params(ctypes.Structure):
                 ("num_node_sample", ctypes.c_int64), ("alpha", ctypes.c_float),
                 ("epsilon", ctypes.c_float), ("eta0", ctypes.c_float), ("eta1", ctypes.c_float),
                 ("a", ctypes.c_double), ("b", ctypes.c_double), ("c", ctypes.c_double),
-                ("seed", ctypes.c_uint32), ("chain", ctypes.c_uint32)]
+                ("seed", ctypes.c_uint32), ("chain", ctypes.c_uint32),
+                ("max_source", ctypes.c_int64)]
 
 
 _lib = None
@@ -116,17 +117,18 @@ class OracleGraph:
         return bool(lib().oracle_is_excluded(ctypes.byref(self.g), int(a), int(b)))
 
 
-def sample_minibatch(og, strategy, m, num_total_edges, seed, chain, step, max_edges):
+def sample_minibatch(og, strategy, m, num_total_edges, seed, chain, step, max_edges,
+                     max_source=1):
     ea = np.zeros(max_edges, np.int32)
     eb = np.zeros(max_edges, np.int32)
     ey = np.zeros(max_edges, np.uint8)
-    nodes = np.zeros(max_edges + 1, np.int32)
+    nodes = np.zeros(2 * max_edges + 1, np.int32)
     info = MbInfo()
-    rc = lib().oracle_sample_minibatch(
-        ctypes.byref(og.g), ctypes.c_int(strategy), ctypes.c_int64(m),
+    rc = lib().oracle_sample_minibatch_ex(
+        ctypes.byref(og.g), ctypes.c_int(strategy), ctypes.c_int64(m), ctypes.c_int64(max_source),
         ctypes.c_int64(num_total_edges), ctypes.c_uint32(seed), ctypes.c_uint32(chain),
         ctypes.c_uint32(step), _p(ea), _p(eb), _p(ey), ctypes.c_int32(max_edges), _p(nodes),
-        ctypes.c_int32(max_edges + 1), ctypes.byref(info))
+        ctypes.c_int32(2 * max_edges + 1), ctypes.byref(info))
     if rc != 0:
         raise RuntimeError("oracle minibatch sampling failed: %d" % rc)
     e, n = info.n_edges, info.n_nodes
@@ -260,7 +262,7 @@ class OracleSampler:
 
     def __init__(self, network, K, strategy=0, mini_batch_size=None, num_node_sample=None,
                  alpha=0.0, epsilon=1e-7, eta0=1.0, eta1=1.0, a=0.0, b=1024.0, c=0.5, seed=42,
-                 chain=0):
+                 chain=0, max_source=1):
         N = network.N
         self.og = OracleGraph(network)
         self.network = network
@@ -270,7 +272,7 @@ class OracleSampler:
             alpha = 1.0 / K
         self.p = Params(K, N, network.num_total_edges, strategy,
                         mini_batch_size or N // 10, num_node_sample or N // 50, alpha, epsilon,
-                        eta0, eta1, a, b, c, seed & 0xffffffff, chain)
+                        eta0, eta1, a, b, c, seed & 0xffffffff, chain, max_source)
         self.K, self.N = K, N
         self.step_count = 1
         self.average_count = 1

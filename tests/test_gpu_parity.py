@@ -88,7 +88,8 @@ def check_sampling(s, net, opts, steps):
         s.step(1)
         got = s.last_minibatch()
         want = oracle.sample_minibatch(og, opts.strategy, m, net.num_total_edges,
-                                       opts.random_seed, opts.chain, step, s.max_edges)
+                                       opts.random_seed, opts.chain, step, s.max_edges,
+                                       max_source=opts.sampler_max_source)
         assert got["flag"] == want["flag"]
         assert got["scale"] == pytest.approx(want["scale"], rel=0, abs=0)
         for k in ("edge_a", "edge_b", "edge_y", "nodes"):
@@ -116,6 +117,52 @@ def test_sampling_link_stratum_redraws_empty(sparse_net):
     s.set_state(*random_state(sparse_net.N, 16))
     check_sampling(s, sparse_net, opts, steps=10)
     s.close()
+
+
+@pytest.mark.parametrize("m", [300, 1000])
+def test_sampling_random_edge(small, m):
+    """random-edge (network.cc:237-268): m distinct training edges drawn from
+    the symmetric CSR, nodes numbered by first appearance."""
+    net, _ = small
+    s, opts = make_sampler(net, strategy=3, mini_batch_size=m)
+    s.set_state(*random_state(net.N, 32))
+    check_sampling(s, net, opts, steps=4)
+    s.close()
+
+
+def test_sampling_random_edge_full_training_set(native_lib):
+    """m at least the training edges: the whole training set is the
+    minibatch (network.cc:215-234, 238-241)."""
+    net = Network.synthetic(n=300, k_true=6, size_min=10, size_max=60, intra_degree=3.0, seed=7)
+    net.make_held_out(0.1, seed=7)
+    s, opts = make_sampler(net, K=8, num_node_sample=8, strategy=3,
+                           mini_batch_size=net.num_total_edges)
+    s.set_state(*random_state(net.N, 8))
+    check_sampling(s, net, opts, steps=2)
+    mb = s.last_minibatch()
+    train = net.num_total_edges - int(net.held_out[2].sum()) - int(net.test[2].sum())
+    assert len(mb["edge_a"]) == train
+    s.close()
+
+
+@pytest.mark.parametrize("strategy", [0, 1])
+def test_sampling_several_link_sources(small, strategy):
+    """sampler.max-source > 1 (network.cc:355-407): several sources per
+    link-stratum attempt, shared edges kept once."""
+    net, _ = small
+    s, opts = make_sampler(net, strategy=strategy, sampler_max_source=5, mini_batch_size=60)
+    s.set_state(*random_state(net.N, 32))
+    check_sampling(s, net, opts, steps=8)
+    s.close()
+
+
+def test_step_random_edge_and_several_sources_against_oracle(small):
+    """A fed update over the general minibatches: random-edge and
+    several link sources (edges between arbitrary node slots)."""
+    net, _ = small
+    for kw in (dict(strategy=3, mini_batch_size=200), dict(strategy=1, sampler_max_source=4,
+                                                           mini_batch_size=60)):
+        run_fed_case(net, 32, 11, _native.PI_F32, **kw)
 
 
 def test_sampling_small_population_collisions(native_lib):
@@ -219,8 +266,10 @@ def check_theta(s, K, theta, mb, tn, step, want_th, want_bt, f_th, f_bt):
     assert np.allclose(gbt, bt_from_th, rtol=1e-6)
 
 
-def run_fed_case(net, K, step, dtype, strategy=0, mini_batch_size=None, num_node_sample=32):
-    kw = dict(K=K, num_node_sample=num_node_sample)
+def run_fed_case(net, K, step, dtype, strategy=0, mini_batch_size=None, num_node_sample=32,
+                 sampler_max_source=1):
+    kw = dict(K=K, num_node_sample=num_node_sample, strategy=strategy,
+              sampler_max_source=sampler_max_source)
     if mini_batch_size:
         kw["mini_batch_size"] = mini_batch_size
     s, opts = make_sampler(net, dtype, **kw)
@@ -229,7 +278,8 @@ def run_fed_case(net, K, step, dtype, strategy=0, mini_batch_size=None, num_node
     pi_dev = s.pi  # the stored pi the kernel gathers neighbour rows from
     og = oracle.OracleGraph(net)
     mb = oracle.sample_minibatch(og, strategy, s.resolved.mini_batch_size, net.num_total_edges,
-                                 opts.random_seed, 0, step, s.max_edges)
+                                 opts.random_seed, 0, step, s.max_edges,
+                                 max_source=sampler_max_source)
     n_out = s.num_node_sample + 1
     nbrs = np.zeros((len(mb["nodes"]), n_out), np.int32)
     nby = np.zeros_like(nbrs, dtype=np.uint8)
