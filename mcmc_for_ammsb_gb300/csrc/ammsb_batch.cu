@@ -403,7 +403,7 @@ int ammsb_batch_step(ammsb_batch* bt, int64_t n_iters) {
   bool in_sync = bt->prefetched;
   for (size_t i = 0; i < bt->h.size() && in_sync; ++i) {
     ammsb_handle* h = bt->h[i];
-    in_sync = h->prefetched && h->parity == bt->parity && h->step_count == bt->expect_step[i];
+    in_sync = h->ahead >= 1 && h->slot == bt->parity && h->step_count == bt->expect_step[i];
   }
   for (ammsb_handle* h : bt->h) BK(cudaStreamSynchronize(h->stream));
   if (!in_sync) {
@@ -413,7 +413,7 @@ int ammsb_batch_step(ammsb_batch* bt, int64_t n_iters) {
         bt->err = h->err;
         return rc;
       }
-      h->parity = 0;
+      h->slot = 0;
       BK(cudaStreamSynchronize(h->stream));
     }
     bt->parity = 0;
@@ -442,8 +442,8 @@ int ammsb_batch_step(ammsb_batch* bt, int64_t n_iters) {
     ammsb_handle* h = bt->h[i];
     BK(cudaStreamWaitEvent(h->stream, bt->ev_done, 0));  // later work on the chain's own stream
     h->step_count += (uint64_t)n_iters;
-    h->parity = bt->parity;
-    h->prefetched = true;
+    h->slot = bt->parity;
+    h->ahead = 1;  // the batch draws one iteration ahead, into buffer sets 0 and 1
     h->last = bt->parity ^ 1;
     bt->expect_step[i] = h->step_count;
   }

@@ -198,16 +198,21 @@ cudaError_t launch_sampling_phase(ammsb_handle* h, const Buffers& b, cudaStream_
   return cudaGetLastError();
 }
 
-// One pipelined iteration on buffer set p: the update of p on the handle's
-// stream, concurrently with the draws of the next iteration into 1 - p on
-// the side stream (fork/join by events; inside a capture these become graph
-// edges).
-cudaError_t launch_pipelined(ammsb_handle* h, int p) {
+// `n` (1 or 2) pipelined iterations from ring slot s: the updates of slots
+// s .. s+n-1 on the handle's stream, concurrently with the draws of the
+// iterations two ahead (slots s+2 .. s+n+1) on the side stream (fork/join by
+// events; inside a capture these become graph edges).  Draws depend only on
+// the step index, so they can run ahead; taking two iterations per join
+// lets the short updates of link-stratum iterations and the longer draws of
+// the non-link ones even out.
+cudaError_t launch_pipelined(ammsb_handle* h, int s, int n) {
   cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
   if (e != cudaSuccess) return e;
   if ((e = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess) return e;
-  if ((e = launch_update_phase(h, h->bufs[p])) != cudaSuccess) return e;
-  if ((e = launch_sampling_phase(h, h->bufs[1 - p], h->side)) != cudaSuccess) return e;
+  for (int i = 0; i < n; ++i)
+    if ((e = launch_update_phase(h, h->bufs[(s + i) % kRing])) != cudaSuccess) return e;
+  for (int i = 0; i < n; ++i)
+    if ((e = launch_sampling_phase(h, h->bufs[(s + 2 + i) % kRing], h->side)) != cudaSuccess) return e;
   if ((e = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess) return e;
   return cudaStreamWaitEvent(h->stream, h->ev_join, 0);
 }
@@ -228,8 +233,8 @@ int check_device_err(ammsb_handle* h) {
 // Drops draws made ahead of time (their step no longer follows) and points
 // the device's next draw at the host's step_count.
 int invalidate_prefetch(ammsb_handle* h) {
-  if (!h->prefetched) return AMMSB_OK;
-  h->prefetched = false;
+  if (h->ahead == 0) return AMMSB_OK;
+  h->ahead = 0;
   uint32_t s = (uint32_t)h->step_count;
   CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
   return AMMSB_OK;
@@ -239,13 +244,13 @@ int reset_counters(ammsb_handle* h) {
   h->step_count = 1;
   h->average_count = 1;
   h->ppx_history.clear();
-  h->parity = 0;
-  h->prefetched = false;
+  h->slot = 0;
+  h->ahead = 0;
   h->last = -1;
   DevCounters gc{};
   gc.next_step = 1;
   CK(cudaMemcpyAsync(h->gc, &gc, sizeof(gc), cudaMemcpyHostToDevice, h->stream));
-  for (int p = 0; p < 2; ++p) CK(cudaMemsetAsync(h->bufs[p].st, 0, sizeof(DevState), h->stream));
+  for (int p = 0; p < kRing; ++p) CK(cudaMemsetAsync(h->bufs[p].st, 0, sizeof(DevState), h->stream));
   CK(cudaMemsetAsync(h->d_ppx, 0, sizeof(float) * std::max<int64_t>(h->H, 1), h->stream));
   return AMMSB_OK;
 }
@@ -322,7 +327,9 @@ const char* ammsb_last_error(const ammsb_handle* h) { return h ? h->err.c_str() 
 void ammsb_destroy(ammsb_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
-  for (auto& g : h->graph_exec)
+  for (auto& g : h->graph1)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto& g : h->graph2)
     if (g) cudaGraphExecDestroy(g);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->side) cudaStreamSynchronize(h->side);
@@ -552,7 +559,7 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   TRY(dev_alloc(h, &b.stage, (size_t)m.max_nodes * Kp));
   TRY(dev_alloc(h, &b.beta, (size_t)Kp));
   TRY(dev_alloc(h, &b.theta, 2 * (size_t)K));
-  for (int p = 0; p < 2; ++p) {  // ping-pong minibatch buffer sets
+  for (int p = 0; p < kRing; ++p) {  // the ring of minibatch buffer sets
     Buffers& bp = h->bufs[p];
     TRY(dev_alloc(h, &bp.nodes, (size_t)m.max_nodes));
     TRY(dev_alloc(h, &bp.ea, (size_t)m.max_edges));
@@ -584,7 +591,7 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   TRY(dev_alloc(h, &h->d_fed_theta_noise, 2 * (size_t)K));
   b.fed_phi_noise = nullptr;
   b.fed_theta_noise = nullptr;
-  for (int p = 0; p < 2; ++p) {  // shared state + this set's minibatch arrays
+  for (int p = 0; p < kRing; ++p) {  // shared state + this set's minibatch arrays
     Buffers own = h->bufs[p];
     h->bufs[p] = b;
     h->bufs[p].nodes = own.nodes;
@@ -703,7 +710,7 @@ int ammsb_set_step(ammsb_handle* h, uint64_t step_count) {
   if (!h || step_count < 1 || step_count > 0xffffffffull) return AMMSB_E_ARG;
   CK(cudaSetDevice(h->device));
   h->step_count = step_count;
-  h->prefetched = false;
+  h->ahead = 0;
   uint32_t s = (uint32_t)step_count;
   CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -718,31 +725,36 @@ int ammsb_step(ammsb_handle* h, int64_t n_iters) {
   }
   CK(cudaSetDevice(h->device));
   if (n_iters == 0) return AMMSB_OK;
-  if (!h->prefetched) {  // draws of the first iteration of this call
-    CK(launch_sampling_phase(h, h->bufs[h->parity], h->stream));
-    h->prefetched = true;
+  // the draws of the next two iterations, where they are not made yet
+  while (h->ahead < 2) {
+    CK(launch_sampling_phase(h, h->bufs[(h->slot + h->ahead) % kRing], h->stream));
+    ++h->ahead;
   }
-  for (int64_t it = 0; it < n_iters; ++it) {
-    const int p = h->parity;
+  int64_t left = n_iters;
+  while (left > 0) {
+    const int n = left >= 2 ? 2 : 1;
+    const int s = h->slot;
     if (h->opt.use_graph) {
-      if (!h->graph_exec[p]) {
+      cudaGraphExec_t& g = (n == 2) ? h->graph2[s] : h->graph1[s];
+      if (!g) {
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = launch_pipelined(h, p);
+        cudaError_t e = launch_pipelined(h, s, n);
         cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
         if (e != cudaSuccess || e2 != cudaSuccess) {
           h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
           return AMMSB_E_CUDA;
         }
-        CK(cudaGraphInstantiate(&h->graph_exec[p], graph, 0));
+        CK(cudaGraphInstantiate(&g, graph, 0));
         cudaGraphDestroy(graph);
       }
-      CK(cudaGraphLaunch(h->graph_exec[p], h->stream));
+      CK(cudaGraphLaunch(g, h->stream));
     } else {
-      CK(launch_pipelined(h, p));
+      CK(launch_pipelined(h, s, n));
     }
-    h->last = p;
-    h->parity = 1 - p;
+    h->last = (s + n - 1) % kRing;
+    h->slot = (s + n) % kRing;
+    left -= n;
   }
   h->step_count += (uint64_t)n_iters;
   return AMMSB_OK;
@@ -785,7 +797,7 @@ int ammsb_step_fed(ammsb_handle* h, uint32_t step, int32_t n_edges, const int32_
   CK(cudaSetDevice(h->device));
   int rc0 = invalidate_prefetch(h);
   if (rc0) return rc0;
-  const Buffers& bp = h->bufs[h->parity];
+  const Buffers& bp = h->bufs[h->slot];
   CK(cudaMemcpyAsync(bp.nodes, nodes, sizeof(int32_t) * n_nodes, cudaMemcpyHostToDevice, h->stream));
   if (n_edges > 0) {
     CK(cudaMemcpyAsync(bp.ea, edge_slot_a, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice, h->stream));
@@ -807,7 +819,7 @@ int ammsb_step_fed(ammsb_handle* h, uint32_t step, int32_t n_edges, const int32_
   fb.fed_phi_noise = h->d_fed_phi_noise;
   fb.fed_theta_noise = h->d_fed_theta_noise;
   CK(launch_update_phase(h, fb));
-  h->last = h->parity;
+  h->last = h->slot;
   return check_device_err(h);
 }
 
@@ -1005,7 +1017,7 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
   CK(cudaSetDevice(h->device));
   int rc0 = invalidate_prefetch(h);
   if (rc0) return rc0;
-  const Buffers& bp = h->bufs[h->parity];
+  const Buffers& bp = h->bufs[h->slot];
   cudaEvent_t ev[6];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaEventRecord(ev[0], h->stream));
@@ -1028,7 +1040,7 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
   }
   for (auto& e : ev) cudaEventDestroy(e);
   h->step_count += 1;
-  h->last = h->parity;
+  h->last = h->slot;
   return check_device_err(h);
 }
 
@@ -1095,11 +1107,12 @@ int apply_phi_cfg(ammsb_handle* h, const KernelCfg& c) {
       return AMMSB_E_CUDA;
     }
   }
-  for (auto& g : h->graph_exec)  // the captured iterations used the old kernels
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (auto* gs : {h->graph1, h->graph2})  // the captured iterations used the old kernels
+    for (int i = 0; i < kRing; ++i)
+      if (gs[i]) {
+        cudaGraphExecDestroy(gs[i]);
+        gs[i] = nullptr;
+      }
   return AMMSB_OK;
 }
 
@@ -1177,8 +1190,8 @@ int ammsb_autotune(ammsb_handle* h, int32_t reps, int32_t flags) {
   // the tuning draws are not an iteration: the next draw is step_count's
   const uint32_t s = (uint32_t)h->step_count;
   CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
-  h->prefetched = false;
-  h->parity = 0;
+  h->ahead = 0;
+  h->slot = 0;
   h->last = -1;
   int rc2 = apply_phi_cfg(h, best);
   CK(cudaStreamSynchronize(h->stream));

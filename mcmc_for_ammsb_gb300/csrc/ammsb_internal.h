@@ -14,6 +14,8 @@
 
 using namespace ammsb;
 
+constexpr int kRing = 4;  // minibatch buffer sets per handle
+
 struct KernelCfg {
   int lpn, vpl, split, npb;  // update_phi
   int tma;                   // wide rows: bulk-copy pipeline kernel
@@ -30,11 +32,11 @@ struct ammsb_handle {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   Model m{};
   DevGraph g{};
-  Buffers b{};        // shared state pointers (bufs[p] add the minibatch buffers)
-  Buffers bufs[2]{};  // ping-pong minibatch buffer sets
+  Buffers b{};        // shared state pointers (bufs[s] add the minibatch buffers)
+  Buffers bufs[kRing]{};  // ring of minibatch buffer sets (draws run two iterations ahead)
   DevCounters* gc = nullptr;
-  int parity = 0;           // buffer set of the next iteration
-  bool prefetched = false;  // bufs[parity] already holds the next iteration's draws
+  int slot = 0;   // ring slot of the next iteration
+  int ahead = 0;  // iterations from `slot` on whose draws are made or queued (0..2)
   int last = -1;            // buffer set of the last applied iteration
   KernelCfg cfg{};
   int64_t E = 0, H = 0, T = 0;
@@ -59,7 +61,9 @@ struct ammsb_handle {
   uint64_t average_count = 1;  // learner.cc:30
   std::vector<double> ppx_history;
   bool state_ready = false;
-  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  // captured iterations per ring slot: one iteration, and two iterations
+  // with the draws of the following two made alongside
+  cudaGraphExec_t graph1[kRing] = {}, graph2[kRing] = {};
   std::string err;
 };
 

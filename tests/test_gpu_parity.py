@@ -480,9 +480,10 @@ def test_errors(small):
     with pytest.raises(_native.AmmsbError) as e:
         MCMCSamplerStochastic(Options(K=0), net).create()
     assert e.value.code == -1
-    with pytest.raises(_native.AmmsbError) as e:
-        MCMCSamplerStochastic(Options(K=16, strategy=3), net).create()
-    assert e.value.code == -6
+    for bad in (dict(strategy=4), dict(sampler_max_source=0), dict(sampler_max_source=5000)):
+        with pytest.raises(_native.AmmsbError) as e:
+            MCMCSamplerStochastic(Options(K=16, **bad), net).create()
+        assert e.value.code == -1
     s, _ = make_sampler(net)
     with pytest.raises(_native.AmmsbError) as e:
         s.step(1)
