@@ -354,6 +354,13 @@ def test_fed_step_ring_depths(wide_net, stages, monkeypatch):
     run_fed_case(wide_net, 1024, 9, _native.PI_BF16, mini_batch_size=64, num_node_sample=40)
 
 
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+@pytest.mark.parametrize("K", [1024, 256])
+def test_fed_step_link_stratum_wide_rows(wide_net, K, dtype):
+    """Few nodes (the link stratum) on the bulk-copy update."""
+    run_fed_case(wide_net, K, 13, dtype, strategy=1, mini_batch_size=64, num_node_sample=40)
+
+
 def test_fed_step_many_nodes_per_cta(wide_net):
     """More minibatch nodes than CTAs of one wave, on the bulk-copy kernel:
     the barriers are re-armed at every node."""
