@@ -116,6 +116,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_over_ranks(secs, evals, world):
+    """Whole-job timing over N replicas: the slowest rank's seconds (max) and
+    the evaluations of all ranks (sum)."""
+    if world <= 1:
+        return secs, evals
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([secs], dtype=torch.float64)
+    e = torch.tensor([evals], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(e, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(e[0])
+
+
 def phi_bytes_per_eval(K, pi_bytes, n_out):
     """Algorithmic bytes of update_phi per sampled edge evaluation: the
     neighbour pi row (K * s_pi) and id (4), plus the node's own traffic
@@ -258,15 +272,7 @@ def ours_arm(args, net, opts, rank, world, local):
     ms = ev_start.elapsed_time(ev_stop)
     e1, i1 = s.counters()
     evals = e1 - e0
-    t = torch.tensor([ms / 1000.0, float(evals)], dtype=torch.float64)
-    if world > 1:
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
-        tsum = t.clone()
-        torch.distributed.all_reduce(tsum[1:], op=torch.distributed.ReduceOp.SUM)
-        secs, total_evals = float(tmax[0]), float(tsum[1])
-    else:
-        secs, total_evals = float(t[0]), float(t[1])
+    secs, total_evals = reduce_over_ranks(ms / 1000.0, float(evals), world)
     value = total_evals / secs
 
     # per-phase CUDA-event durations of the same iteration (not captured),
