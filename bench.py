@@ -207,15 +207,18 @@ def cpu_sample(net, opts, seconds, threads, max_steps=None, per_step_nodes=512,
 
 def reference_arm(args, net, opts):
     threads = os.cpu_count() or 1
-    # warm-up steps, then K timed steps (each a bounded per-iteration sample)
-    cpu_sample(net, opts, 0, threads, max_steps=args.warmup, per_step_nodes=args.ref_nodes)
-    ev, secs, steps, nodes = cpu_sample(net, opts, 0, threads, max_steps=args.steps,
+    # warm-up steps, then timed steps, each a bounded per-iteration sample
+    # (at most 200 iterations are timed, so that the run ends in minutes)
+    timed = min(args.steps, 200)
+    cpu_sample(net, opts, 0, threads, max_steps=min(args.warmup, 5),
+               per_step_nodes=args.ref_nodes)
+    ev, secs, steps, nodes = cpu_sample(net, opts, 0, threads, max_steps=timed,
                                         per_step_nodes=args.ref_nodes, seed=1)
     value = ev / secs
-    sample = ("oracle restatement of neighbour sampling + update_phi, FP32, on up to %d "
-              "minibatch nodes per iteration of the %s workload (%d iterations, %d nodes, "
-              "%d edge evaluations); pi rows from a 2^18-row pool" %
-              (args.ref_nodes, args.workload, steps, nodes, ev))
+    sample = ("oracle restatement of minibatch + neighbour sampling and update_phi, FP32, on "
+              "up to %d minibatch nodes per iteration of the %s workload (%d iterations timed, "
+              "%d nodes, %d edge evaluations, %d host threads); pi rows from a 2^18-row pool" %
+              (args.ref_nodes, args.workload, steps, nodes, ev, threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(steps, 1),
