@@ -19,20 +19,21 @@ enum : int32_t {
 
 // Per-iteration scalars of one minibatch buffer set, resident in device
 // memory so that a captured CUDA graph can replay the iteration without host
-// involvement.  The sampler keeps two buffer sets (ping-pong): the draws of
-// iteration t+1 are made while iteration t updates the state.
+// involvement.  The sampler keeps a ring of buffer sets: the draws of
+// iterations t+2 and t+3 are made while iterations t and t+1 update the
+// state.
 struct DevState {
   uint32_t step;   // step_count of the iteration these draws belong to
   float eps;       // eps_t of that iteration
-  float scale;     // minibatch scale (network.cc:341, 386-390)
-  int32_t flag;    // 0 non-link stratum, 1 link stratum
+  float scale;     // minibatch scale (network.cc:263, 341, 386-390)
+  int32_t flag;    // 0 non-link stratum, 1 link stratum, 2 random-edge
   int32_t n_edges;
   int32_t n_nodes;
   int32_t rounds;
   int32_t pad;
 };
 
-// Sampler-wide counters shared by both buffer sets.
+// Sampler-wide counters shared by all buffer sets.
 struct DevCounters {
   uint32_t next_step;        // step_count the next sampling pass draws for
   int32_t err;               // error bits
