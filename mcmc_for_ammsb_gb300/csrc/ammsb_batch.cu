@@ -34,6 +34,7 @@ struct PhiGroup {
   ChainArgs* d = nullptr;  // the group's chains, in order
   int gx = 1;
   size_t smem = 0;
+  size_t smem_wide = 0;  // bulk-copy kernel: its 16-warp variant
 };
 
 struct CommitGroup {
@@ -55,9 +56,28 @@ cudaError_t phi_reg_chains(const PhiGroup& g, int p, cudaStream_t st) {
 
 template <typename PiT, int V, int STAGES, bool FULL>
 cudaError_t phi_tma_chains(const PhiGroup& g, int p, cudaStream_t st, bool configure) {
+  // the same pair of launches as one chain: a 16-warp variant for the
+  // iterations of few nodes, the 4-warp kernel for the others
+  constexpr int WS = sizeof(PiT) == 2 ? 4 : 2;
   auto kern = k_update_phi_tma_chains<PiT, V, kTmaSplitB, STAGES, FULL>;
-  if (configure) return ammsb_detail::raise_smem_limit(kern, g.smem);
-  kern<<<dim3(g.gx, (unsigned)g.chains.size()), kTmaSplitB * 32, g.smem, st>>>(g.d, p);
+  auto wide = k_update_phi_tma_chains<PiT, V, kTmaSplitWide, WS, FULL>;
+  // every chain of the group configured the variant (its shared memory is
+  // then the largest of theirs), or none did
+  const bool use_wide = g.cfg.tma_few && g.smem_wide > 0 && g.smem_wide <= 200 * 1024;
+  if (configure) {
+    cudaError_t e = ammsb_detail::raise_smem_limit(kern, g.smem);
+    if (e == cudaSuccess && use_wide) e = ammsb_detail::raise_smem_limit(wide, g.smem_wide);
+    return e;
+  }
+  const unsigned n = (unsigned)g.chains.size();
+  if (use_wide) {
+    wide<<<dim3(kTmaFewNodes, n), kTmaSplitWide * 32, g.smem_wide, st>>>(g.d, p, 0, kTmaFewNodes);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    kern<<<dim3(g.gx, n), kTmaSplitB * 32, g.smem, st>>>(g.d, p, kTmaFewNodes, INT32_MAX);
+  } else {
+    kern<<<dim3(g.gx, n), kTmaSplitB * 32, g.smem, st>>>(g.d, p, 0, INT32_MAX);
+  }
   return cudaGetLastError();
 }
 
@@ -315,6 +335,7 @@ int ammsb_batch_create(ammsb_handle* const* handles, int32_t n, ammsb_batch** ou
     if (c.tma) {
       g.gx = std::max(g.gx, h->m.max_nodes);
       g.smem = std::max(g.smem, h->phi_smem);
+      g.smem_wide = std::max(g.smem_wide, h->phi_smem_wide);
     } else {
       const int npb = std::max(1, 128 / (c.lpn * c.split));
       g.gx = std::max(g.gx, std::max(1, std::min((h->m.max_nodes + npb - 1) / npb, 152 * 32)));

@@ -87,14 +87,28 @@ constexpr int kTmaSplit = 4;
 template <typename PiT, int VPL, int STAGES, bool FULL>
 cudaError_t launch_phi_tma_t(ammsb_handle* h, const Buffers& b, bool configure) {
   auto kern = k_update_phi_tma<PiT, VPL, kTmaSplit, STAGES, FULL>;
+  constexpr int WS = sizeof(PiT) == 2 ? 4 : 2;  // ring depth of the 16-warp variant
+  auto wide = k_update_phi_tma<PiT, VPL, kTmaSplitWide, WS, FULL>;
   const size_t smem = PhiTmaSmem<PiT, VPL, kTmaSplit, STAGES>::bytes(h->m.Kp, h->m.n_out);
+  const size_t smem_w = PhiTmaSmem<PiT, VPL, kTmaSplitWide, WS>::bytes(h->m.Kp, h->m.n_out);
+  const bool use_wide = h->cfg.tma_few && smem_w <= 200 * 1024;
   if (configure) {
     cudaError_t e = ammsb_detail::raise_smem_limit(kern, smem);
     if (e != cudaSuccess) return e;
+    if (use_wide && (e = ammsb_detail::raise_smem_limit(wide, smem_w)) != cudaSuccess) return e;
     h->phi_smem = smem;
+    h->phi_smem_wide = use_wide ? smem_w : 0;
     return cudaSuccess;
   }
-  kern<<<h->m.max_nodes, kTmaSplit * 32, smem, h->stream>>>(h->m, b);
+  if (use_wide) {
+    wide<<<std::min(kTmaFewNodes, h->m.max_nodes), kTmaSplitWide * 32, smem_w, h->stream>>>(
+        h->m, b, 0, kTmaFewNodes);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    kern<<<h->m.max_nodes, kTmaSplit * 32, smem, h->stream>>>(h->m, b, kTmaFewNodes, INT32_MAX);
+  } else {
+    kern<<<h->m.max_nodes, kTmaSplit * 32, smem, h->stream>>>(h->m, b, 0, INT32_MAX);
+  }
   return cudaGetLastError();
 }
 
@@ -269,6 +283,8 @@ void choose_config(ammsb_handle* h) {
   c.split = (c.lpn == 32) ? (c.vpl >= 2 ? 4 : 2) : 1;
   c.tma = (c.lpn == 32) ? 1 : 0;
   c.tma_stages = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 4 : 3;  // fastest ring depths on GB300
+  c.tma_few = 1;
+  if (const char* env = std::getenv("AMMSB_PHI_FEW")) c.tma_few = std::atoi(env) != 0;
   if (const char* env = std::getenv("AMMSB_PHI_KERNEL")) {  // "tma" or "regs"
     if (std::strcmp(env, "regs") == 0) c.tma = 0;
   }

@@ -20,6 +20,7 @@ struct KernelCfg {
   int lpn, vpl, split, npb;  // update_phi
   int tma;                   // wide rows: bulk-copy pipeline kernel
   int tma_stages;            // its ring depth
+  int tma_few;               // a 16-warp variant takes iterations of few nodes
   int ppx_lpn, ppx_vpl;      // perplexity
   int kq;                    // commit_beta
 };
@@ -55,7 +56,7 @@ struct ammsb_handle {
   int32_t* d_err_init = nullptr;
   int ncommit = 1;
   int nbr_blocks = 1, phi_blocks = 1;
-  size_t phi_smem = 0, nbr_smem = 0, mb_smem = 0;
+  size_t phi_smem = 0, phi_smem_wide = 0, nbr_smem = 0, mb_smem = 0;
   // host mirrors
   uint64_t step_count = 1;     // learner.cc:37
   uint64_t average_count = 1;  // learner.cc:30
@@ -85,6 +86,11 @@ struct ammsb_handle {
   X(32, 1, 4) X(32, 2, 1) X(32, 2, 2) X(32, 2, 4) X(32, 4, 1) X(32, 4, 2) X(32, 4, 4)   \
   X(32, 8, 1) X(32, 8, 2) X(32, 8, 4) X(16, 1, 2) X(8, 1, 2) X(8, 1, 4) X(16, 2, 1)     \
   X(8, 2, 1) X(8, 4, 1) X(4, 2, 1) X(4, 4, 1)
+
+// Iterations with at most kTmaFewNodes nodes (the link stratum) take a
+// kTmaSplitWide-warp variant of the bulk-copy update_phi kernel.
+constexpr int kTmaFewNodes = 64;
+constexpr int kTmaSplitWide = 16;
 
 // Ring depths the bulk-copy update_phi kernel is built for.
 #define AMMSB_PHI_TMA_STAGES(X) X(3) X(4) X(6)

@@ -420,14 +420,24 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
     __syncthreads();  // smem reuse by the next node
   }
 }
+// The iteration's node count picks the launch that does the work: the
+// kernel runs when n_lo < n_nodes <= n_hi and returns at once otherwise.
+// Iterations with few nodes (the link stratum: one vertex and its edges)
+// take a 16-warp variant, whose warps each hold a quarter of the rows the
+// 4-warp one gives them, so a node's rows are in flight together.
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
-__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1) k_update_phi_tma(Model m, Buffers b) {
+__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1)
+    k_update_phi_tma(Model m, Buffers b, int n_lo, int n_hi) {
+  const int n_nodes = b.st->n_nodes;
+  if (n_nodes <= n_lo || n_nodes > n_hi) return;
   update_phi_tma_body<PiT, VPL, SPLIT, STAGES, FULL>(m, b);
 }
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
 __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1)
-    k_update_phi_tma_chains(const ChainArgs* __restrict__ c, int p) {
+    k_update_phi_tma_chains(const ChainArgs* __restrict__ c, int p, int n_lo, int n_hi) {
   const ChainArgs& a = c[blockIdx.y];
+  const int n_nodes = a.b[p].st->n_nodes;
+  if (n_nodes <= n_lo || n_nodes > n_hi) return;
   update_phi_tma_body<PiT, VPL, SPLIT, STAGES, FULL>(a.m, a.b[p]);
 }
 
