@@ -195,7 +195,7 @@ int ammsb_get_counters(ammsb_handle *h, uint64_t *edge_evals,
 /* Autotuner of the update_phi kernel (no reference counterpart): times
  * every built shape of the kernel that covers this handle's rows -- lanes
  * per node and vectors per lane (the K-tile), sub-groups per node (warps per
- * node), and the bulk-copy kernel's ring depth for wide rows -- `reps`
+ * node), and the ring kernel's depth for wide rows -- `reps`
  * launches each on a non-link minibatch of the handle's own graph against a
  * scratch copy of phi (the chain's state and its draws are untouched), and
  * keeps the fastest.  Choices are cached per (device, pi type, row width,
@@ -203,7 +203,7 @@ int ammsb_get_counters(ammsb_handle *h, uint64_t *edge_evals,
  * again.  Needs a state (ammsb_init_state / ammsb_set_state). */
 #define AMMSB_TUNE_FRESH 1
 int ammsb_autotune(ammsb_handle *h, int32_t reps, int32_t flags);
-/* The update_phi configuration in use: out[0..4] = bulk-copy kernel (0/1),
+/* The update_phi configuration in use: out[0..4] = ring kernel (0/1),
  * lanes per node, vectors per lane, sub-groups per node, ring depth. */
 int ammsb_get_kernel_config(ammsb_handle *h, int32_t *out);
 

@@ -21,7 +21,7 @@
 #include <vector>
 
 #include "ammsb_internal.h"
-#include "ammsb_phi_tma.cuh"
+#include "ammsb_phi_ring.cuh"
 
 namespace {
 
@@ -29,12 +29,12 @@ namespace {
 struct PhiGroup {
   int dtype;
   KernelCfg cfg;
-  bool full;  // bulk-copy kernel: every lane's vectors inside the row
+  bool full;  // ring kernel: every lane's vectors inside the row
   std::vector<int> chains;
   ChainArgs* d = nullptr;  // the group's chains, in order
   int gx = 1;
   size_t smem = 0;
-  size_t smem_wide = 0;  // bulk-copy kernel: its 16-warp variant
+  size_t smem_wide = 0;  // ring kernel: its 16-warp variant
 };
 
 struct CommitGroup {
@@ -44,7 +44,7 @@ struct CommitGroup {
   int gx = 1;
 };
 
-constexpr int kTmaSplitB = 4;
+constexpr int kRingSplitB = 4;
 
 template <typename PiT, int L, int V, int S>
 cudaError_t phi_reg_chains(const PhiGroup& g, int p, cudaStream_t st) {
@@ -55,15 +55,15 @@ cudaError_t phi_reg_chains(const PhiGroup& g, int p, cudaStream_t st) {
 }
 
 template <typename PiT, int V, int STAGES, bool FULL>
-cudaError_t phi_tma_chains(const PhiGroup& g, int p, cudaStream_t st, bool configure) {
+cudaError_t phi_ring_chains(const PhiGroup& g, int p, cudaStream_t st, bool configure) {
   // the same pair of launches as one chain: a 16-warp variant for the
   // iterations of few nodes, the 4-warp kernel for the others
   constexpr int WS = sizeof(PiT) == 2 ? 4 : 2;
-  auto kern = k_update_phi_tma_chains<PiT, V, kTmaSplitB, STAGES, FULL>;
-  auto wide = k_update_phi_tma_chains<PiT, V, kTmaSplitWide, WS, FULL>;
+  auto kern = k_update_phi_ring_chains<PiT, V, kRingSplitB, STAGES, FULL>;
+  auto wide = k_update_phi_ring_chains<PiT, V, kRingSplitWide, WS, FULL>;
   // every chain of the group configured the variant (its shared memory is
   // then the largest of theirs), or none did
-  const bool use_wide = g.cfg.tma_few && g.smem_wide > 0 && g.smem_wide <= 200 * 1024;
+  const bool use_wide = g.cfg.ring_few && g.smem_wide > 0 && g.smem_wide <= 200 * 1024;
   if (configure) {
     cudaError_t e = ammsb_detail::raise_smem_limit(kern, g.smem);
     if (e == cudaSuccess && use_wide) e = ammsb_detail::raise_smem_limit(wide, g.smem_wide);
@@ -71,36 +71,36 @@ cudaError_t phi_tma_chains(const PhiGroup& g, int p, cudaStream_t st, bool confi
   }
   const unsigned n = (unsigned)g.chains.size();
   if (use_wide) {
-    wide<<<dim3(kTmaFewNodes, n), kTmaSplitWide * 32, g.smem_wide, st>>>(g.d, p, 0, kTmaFewNodes);
+    wide<<<dim3(kRingFewNodes, n), kRingSplitWide * 32, g.smem_wide, st>>>(g.d, p, 0, kRingFewNodes);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    kern<<<dim3(g.gx, n), kTmaSplitB * 32, g.smem, st>>>(g.d, p, kTmaFewNodes, INT32_MAX);
+    kern<<<dim3(g.gx, n), kRingSplitB * 32, g.smem, st>>>(g.d, p, kRingFewNodes, INT32_MAX);
   } else {
-    kern<<<dim3(g.gx, n), kTmaSplitB * 32, g.smem, st>>>(g.d, p, 0, INT32_MAX);
+    kern<<<dim3(g.gx, n), kRingSplitB * 32, g.smem, st>>>(g.d, p, 0, INT32_MAX);
   }
   return cudaGetLastError();
 }
 
 template <typename PiT, int V>
-cudaError_t phi_tma_chains_v(const PhiGroup& g, int p, cudaStream_t st, bool configure) {
-#define TMA_CASE(S)                                                                           \
-  if (g.cfg.tma_stages == S)                                                                  \
-    return g.full ? phi_tma_chains<PiT, V, S, true>(g, p, st, configure)                      \
-                  : phi_tma_chains<PiT, V, S, false>(g, p, st, configure);
-  AMMSB_PHI_TMA_STAGES(TMA_CASE)
-#undef TMA_CASE
+cudaError_t phi_ring_chains_v(const PhiGroup& g, int p, cudaStream_t st, bool configure) {
+#define RING_CASE(S)                                                                           \
+  if (g.cfg.ring_stages == S)                                                                  \
+    return g.full ? phi_ring_chains<PiT, V, S, true>(g, p, st, configure)                      \
+                  : phi_ring_chains<PiT, V, S, false>(g, p, st, configure);
+  AMMSB_PHI_RING_STAGES(RING_CASE)
+#undef RING_CASE
   return cudaErrorInvalidConfiguration;
 }
 
 template <typename PiT>
 cudaError_t phi_chains(const PhiGroup& g, int p, cudaStream_t st, bool configure) {
   const KernelCfg& c = g.cfg;
-  if (c.tma) {
+  if (c.ring) {
     switch (c.vpl) {
-      case 1: return phi_tma_chains_v<PiT, 1>(g, p, st, configure);
-      case 2: return phi_tma_chains_v<PiT, 2>(g, p, st, configure);
-      case 4: return phi_tma_chains_v<PiT, 4>(g, p, st, configure);
-      case 8: return phi_tma_chains_v<PiT, 8>(g, p, st, configure);
+      case 1: return phi_ring_chains_v<PiT, 1>(g, p, st, configure);
+      case 2: return phi_ring_chains_v<PiT, 2>(g, p, st, configure);
+      case 4: return phi_ring_chains_v<PiT, 4>(g, p, st, configure);
+      case 8: return phi_ring_chains_v<PiT, 8>(g, p, st, configure);
       default: return cudaErrorInvalidConfiguration;
     }
   }
@@ -319,8 +319,8 @@ int ammsb_batch_create(ammsb_handle* const* handles, int32_t n, ammsb_batch** ou
     const KernelCfg& c = h->cfg;
     const int ev = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 8 : 4;
     const bool full = (h->m.Kp / ev == 32 * c.vpl);
-    auto key = std::make_tuple((int)h->opt.pi_dtype, c.tma, c.lpn, c.vpl, c.split,
-                               c.tma ? c.tma_stages : 0, c.tma ? (int)full : 0);
+    auto key = std::make_tuple((int)h->opt.pi_dtype, c.ring, c.lpn, c.vpl, c.split,
+                               c.ring ? c.ring_stages : 0, c.ring ? (int)full : 0);
     auto it = pg.find(key);
     if (it == pg.end()) {
       PhiGroup g;
@@ -332,7 +332,7 @@ int ammsb_batch_create(ammsb_handle* const* handles, int32_t n, ammsb_batch** ou
     }
     PhiGroup& g = bt->phi[it->second];
     g.chains.push_back(i);
-    if (c.tma) {
+    if (c.ring) {
       g.gx = std::max(g.gx, h->m.max_nodes);
       g.smem = std::max(g.smem, h->phi_smem);
       g.smem_wide = std::max(g.smem_wide, h->phi_smem_wide);

@@ -19,7 +19,7 @@
 #include <vector>
 
 #include "ammsb_internal.h"
-#include "ammsb_phi_tma.cuh"
+#include "ammsb_phi_ring.cuh"
 
 namespace {
 thread_local std::string g_create_error;
@@ -82,16 +82,16 @@ cudaError_t launch_phi_t(ammsb_handle* h, const Buffers& b) {
   return cudaGetLastError();
 }
 
-constexpr int kTmaSplit = 4;
+constexpr int kRingSplit = 4;
 
 template <typename PiT, int VPL, int STAGES, bool FULL>
-cudaError_t launch_phi_tma_t(ammsb_handle* h, const Buffers& b, bool configure) {
-  auto kern = k_update_phi_tma<PiT, VPL, kTmaSplit, STAGES, FULL>;
+cudaError_t launch_phi_ring_t(ammsb_handle* h, const Buffers& b, bool configure) {
+  auto kern = k_update_phi_ring<PiT, VPL, kRingSplit, STAGES, FULL>;
   constexpr int WS = sizeof(PiT) == 2 ? 4 : 2;  // ring depth of the 16-warp variant
-  auto wide = k_update_phi_tma<PiT, VPL, kTmaSplitWide, WS, FULL>;
-  const size_t smem = PhiTmaSmem<PiT, VPL, kTmaSplit, STAGES>::bytes(h->m.Kp, h->m.n_out);
-  const size_t smem_w = PhiTmaSmem<PiT, VPL, kTmaSplitWide, WS>::bytes(h->m.Kp, h->m.n_out);
-  const bool use_wide = h->cfg.tma_few && smem_w <= 200 * 1024;
+  auto wide = k_update_phi_ring<PiT, VPL, kRingSplitWide, WS, FULL>;
+  const size_t smem = PhiRingSmem<PiT, VPL, kRingSplit, STAGES>::bytes(h->m.Kp, h->m.n_out);
+  const size_t smem_w = PhiRingSmem<PiT, VPL, kRingSplitWide, WS>::bytes(h->m.Kp, h->m.n_out);
+  const bool use_wide = h->cfg.ring_few && smem_w <= 200 * 1024;
   if (configure) {
     cudaError_t e = ammsb_detail::raise_smem_limit(kern, smem);
     if (e != cudaSuccess) return e;
@@ -101,39 +101,39 @@ cudaError_t launch_phi_tma_t(ammsb_handle* h, const Buffers& b, bool configure) 
     return cudaSuccess;
   }
   if (use_wide) {
-    wide<<<std::min(kTmaFewNodes, h->m.max_nodes), kTmaSplitWide * 32, smem_w, h->stream>>>(
-        h->m, b, 0, kTmaFewNodes);
+    wide<<<std::min(kRingFewNodes, h->m.max_nodes), kRingSplitWide * 32, smem_w, h->stream>>>(
+        h->m, b, 0, kRingFewNodes);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    kern<<<h->m.max_nodes, kTmaSplit * 32, smem, h->stream>>>(h->m, b, kTmaFewNodes, INT32_MAX);
+    kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, kRingFewNodes, INT32_MAX);
   } else {
-    kern<<<h->m.max_nodes, kTmaSplit * 32, smem, h->stream>>>(h->m, b, 0, INT32_MAX);
+    kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, 0, INT32_MAX);
   }
   return cudaGetLastError();
 }
 
-// ring depths the bulk-copy kernel is built for; FULL when every lane's
+// ring depths the ring kernel is built for; FULL when every lane's
 // vectors lie inside the row
 template <typename PiT, int VPL>
-cudaError_t launch_phi_tma_v(ammsb_handle* h, const Buffers& b, bool configure) {
+cudaError_t launch_phi_ring_v(ammsb_handle* h, const Buffers& b, bool configure) {
   constexpr int EV = PiTraits<PiT>::kPerVec;
   const bool full = (h->m.Kp / EV == 32 * VPL);
-#define TMA_CASE(S)                                                                        \
-  if (h->cfg.tma_stages == S)                                                              \
-    return full ? launch_phi_tma_t<PiT, VPL, S, true>(h, b, configure)                     \
-                : launch_phi_tma_t<PiT, VPL, S, false>(h, b, configure);
-  AMMSB_PHI_TMA_STAGES(TMA_CASE)
-#undef TMA_CASE
+#define RING_CASE(S)                                                                        \
+  if (h->cfg.ring_stages == S)                                                              \
+    return full ? launch_phi_ring_t<PiT, VPL, S, true>(h, b, configure)                     \
+                : launch_phi_ring_t<PiT, VPL, S, false>(h, b, configure);
+  AMMSB_PHI_RING_STAGES(RING_CASE)
+#undef RING_CASE
   return cudaErrorInvalidConfiguration;
 }
 
 template <typename PiT>
-cudaError_t launch_phi_tma(ammsb_handle* h, const Buffers& b, bool configure) {
+cudaError_t launch_phi_ring(ammsb_handle* h, const Buffers& b, bool configure) {
   switch (h->cfg.vpl) {
-    case 1: return launch_phi_tma_v<PiT, 1>(h, b, configure);
-    case 2: return launch_phi_tma_v<PiT, 2>(h, b, configure);
-    case 4: return launch_phi_tma_v<PiT, 4>(h, b, configure);
-    case 8: return launch_phi_tma_v<PiT, 8>(h, b, configure);
+    case 1: return launch_phi_ring_v<PiT, 1>(h, b, configure);
+    case 2: return launch_phi_ring_v<PiT, 2>(h, b, configure);
+    case 4: return launch_phi_ring_v<PiT, 4>(h, b, configure);
+    case 8: return launch_phi_ring_v<PiT, 8>(h, b, configure);
     default: return cudaErrorInvalidConfiguration;
   }
 }
@@ -141,7 +141,7 @@ cudaError_t launch_phi_tma(ammsb_handle* h, const Buffers& b, bool configure) {
 template <typename PiT>
 cudaError_t launch_phi(ammsb_handle* h, const Buffers& b) {
   const KernelCfg& c = h->cfg;
-  if (c.tma) return launch_phi_tma<PiT>(h, b, false);
+  if (c.ring) return launch_phi_ring<PiT>(h, b, false);
 #define PHI_CASE(L, V, S) \
   if (c.lpn == L && c.vpl == V && c.split == S) return launch_phi_t<PiT, L, V, S>(h, b);
   AMMSB_PHI_REG_SHAPES(PHI_CASE)
@@ -281,16 +281,16 @@ void choose_config(ammsb_handle* h) {
     c.vpl = next_pow2((nvec + 31) / 32);
   }
   c.split = (c.lpn == 32) ? (c.vpl >= 2 ? 4 : 2) : 1;
-  c.tma = (c.lpn == 32) ? 1 : 0;
-  c.tma_stages = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 4 : 3;  // fastest ring depths on GB300
-  c.tma_few = 1;
-  if (const char* env = std::getenv("AMMSB_PHI_FEW")) c.tma_few = std::atoi(env) != 0;
-  if (const char* env = std::getenv("AMMSB_PHI_KERNEL")) {  // "tma" or "regs"
-    if (std::strcmp(env, "regs") == 0) c.tma = 0;
+  c.ring = (c.lpn == 32) ? 1 : 0;
+  c.ring_stages = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 4 : 3;  // fastest ring depths on GB300
+  c.ring_few = 1;
+  if (const char* env = std::getenv("AMMSB_PHI_FEW")) c.ring_few = std::atoi(env) != 0;
+  if (const char* env = std::getenv("AMMSB_PHI_KERNEL")) {  // "ring" or "regs"
+    if (std::strcmp(env, "regs") == 0) c.ring = 0;
   }
-  if (const char* env = std::getenv("AMMSB_PHI_TMA")) {  // ring stages
+  if (const char* env = std::getenv("AMMSB_PHI_RING")) {  // ring stages
     int st = 0;
-    if (std::sscanf(env, "%d", &st) == 1) c.tma_stages = st;
+    if (std::sscanf(env, "%d", &st) == 1) c.ring_stages = st;
   }
   c.npb = std::max(1, 128 / (c.lpn * c.split));
   c.ppx_lpn = c.lpn;
@@ -633,9 +633,9 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
       return bail(AMMSB_E_ARG);
     }
   }
-  if (h->cfg.tma) {
-    cudaError_t e = (o.pi_dtype == AMMSB_PI_BF16) ? launch_phi_tma<__nv_bfloat16>(h, h->b, true)
-                                                   : launch_phi_tma<float>(h, h->b, true);
+  if (h->cfg.ring) {
+    cudaError_t e = (o.pi_dtype == AMMSB_PI_BF16) ? launch_phi_ring<__nv_bfloat16>(h, h->b, true)
+                                                   : launch_phi_ring<float>(h, h->b, true);
     if (e != cudaSuccess) {
       h->err = std::string("update_phi shared memory configuration: ") + cudaGetErrorString(e);
       return bail(AMMSB_E_CUDA);
@@ -653,7 +653,7 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
     std::fprintf(stderr, "num_node_sample %lld\na %g b %g c %g eta (%g,%g)\n",
                  (long long)o.num_node_sample, o.a, o.b, o.c, o.eta0, o.eta1);
     std::fprintf(stderr, "update_phi lanes/node %d vec/lane %d split %d %s; pi %s\n", h->cfg.lpn,
-                 h->cfg.vpl, h->cfg.split, h->cfg.tma ? "bulk-copy pipeline" : "register path",
+                 h->cfg.vpl, h->cfg.split, h->cfg.ring ? "shared-memory ring" : "register path",
                  o.pi_dtype == AMMSB_PI_BF16 ? "bf16" : "f32");
   }
   *out = h;
@@ -1063,7 +1063,7 @@ int ammsb_profile_step(ammsb_handle* h, double* ms5) {
 // ---------------------------------------------------------------------------
 // Autotuner of update_phi: warps-per-node and K-tile.  Every built shape of
 // the kernels that covers this handle's row (lanes x vectors per lane within
-// 2x of the row's 16-byte vectors; the bulk-copy kernel at each ring depth
+// 2x of the row's 16-byte vectors; the ring kernel at each ring depth
 // for wide rows) is timed with CUDA events on a non-link minibatch of this
 // handle's graph, against a scratch copy of phi so the chain's state is not
 // touched; the fastest becomes the handle's configuration.  Choices are
@@ -1081,7 +1081,7 @@ std::vector<KernelCfg> phi_candidates(const ammsb_handle* h) {
   const int nvec = h->m.Kp / ev;
   std::vector<KernelCfg> out;
   KernelCfg base = h->cfg;
-  base.tma = 0;
+  base.ring = 0;
 #define CAND(L, V, S)                                                      \
   if ((L) * (V) >= nvec && (L) * (V) < 2 * nvec + ((L) == 1 ? 1 : 0)) {  \
     KernelCfg c = base;                                                    \
@@ -1098,14 +1098,14 @@ std::vector<KernelCfg> phi_candidates(const ammsb_handle* h) {
 #define TCAND(S)          \
   {                       \
     KernelCfg c = base;   \
-    c.tma = 1;            \
+    c.ring = 1;            \
     c.lpn = 32;           \
     c.vpl = vpl;          \
     c.split = 4;          \
-    c.tma_stages = S;     \
+    c.ring_stages = S;     \
     out.push_back(c);     \
   }
-      AMMSB_PHI_TMA_STAGES(TCAND)
+      AMMSB_PHI_RING_STAGES(TCAND)
 #undef TCAND
     }
   }
@@ -1115,9 +1115,9 @@ std::vector<KernelCfg> phi_candidates(const ammsb_handle* h) {
 int apply_phi_cfg(ammsb_handle* h, const KernelCfg& c) {
   h->cfg = c;
   h->cfg.npb = std::max(1, 128 / (c.lpn * c.split));
-  if (c.tma) {
-    cudaError_t e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_phi_tma<__nv_bfloat16>(h, h->b, true)
-                                                       : launch_phi_tma<float>(h, h->b, true);
+  if (c.ring) {
+    cudaError_t e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_phi_ring<__nv_bfloat16>(h, h->b, true)
+                                                       : launch_phi_ring<float>(h, h->b, true);
     if (e != cudaSuccess) {
       h->err = std::string("update_phi configuration: ") + cudaGetErrorString(e);
       return AMMSB_E_CUDA;
@@ -1222,11 +1222,11 @@ int ammsb_autotune(ammsb_handle* h, int32_t reps, int32_t flags) {
 
 int ammsb_get_kernel_config(ammsb_handle* h, int32_t* out) {
   if (!h || !out) return AMMSB_E_ARG;
-  out[0] = h->cfg.tma;
+  out[0] = h->cfg.ring;
   out[1] = h->cfg.lpn;
   out[2] = h->cfg.vpl;
   out[3] = h->cfg.split;
-  out[4] = h->cfg.tma_stages;
+  out[4] = h->cfg.ring_stages;
   return AMMSB_OK;
 }
 

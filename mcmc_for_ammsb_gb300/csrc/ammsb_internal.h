@@ -18,9 +18,9 @@ constexpr int kRing = 4;  // minibatch buffer sets per handle
 
 struct KernelCfg {
   int lpn, vpl, split, npb;  // update_phi
-  int tma;                   // wide rows: bulk-copy pipeline kernel
-  int tma_stages;            // its ring depth
-  int tma_few;               // a 16-warp variant takes iterations of few nodes
+  int ring;                  // wide rows: the shared-memory ring kernel
+  int ring_stages;           // its ring depth
+  int ring_few;              // a 16-warp variant takes iterations of few nodes
   int ppx_lpn, ppx_vpl;      // perplexity
   int kq;                    // commit_beta
 };
@@ -87,13 +87,13 @@ struct ammsb_handle {
   X(32, 8, 1) X(32, 8, 2) X(32, 8, 4) X(16, 1, 2) X(8, 1, 2) X(8, 1, 4) X(16, 2, 1)     \
   X(8, 2, 1) X(8, 4, 1) X(4, 2, 1) X(4, 4, 1)
 
-// Iterations with at most kTmaFewNodes nodes (the link stratum) take a
-// kTmaSplitWide-warp variant of the bulk-copy update_phi kernel.
-constexpr int kTmaFewNodes = 64;
-constexpr int kTmaSplitWide = 16;
+// Iterations with at most kRingFewNodes nodes (the link stratum) take a
+// kRingSplitWide-warp variant of the ring update_phi kernel.
+constexpr int kRingFewNodes = 64;
+constexpr int kRingSplitWide = 16;
 
-// Ring depths the bulk-copy update_phi kernel is built for.
-#define AMMSB_PHI_TMA_STAGES(X) X(3) X(4) X(6)
+// Ring depths the ring update_phi kernel is built for.
+#define AMMSB_PHI_RING_STAGES(X) X(3) X(4) X(6)
 
 namespace ammsb_detail {
 // Raises a kernel's dynamic shared memory limit to at least `bytes` and

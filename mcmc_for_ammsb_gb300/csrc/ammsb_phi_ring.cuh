@@ -1,79 +1,24 @@
-// ammsb_phi_tma.cuh -- update_phi for wide pi rows (>= 512 bytes), with the
-// neighbour rows staged in shared memory by the Blackwell bulk-copy engine.
+// ammsb_phi_ring.cuh -- update_phi for wide pi rows (>= 512 bytes), with the
+// neighbour rows staged in shared memory through a per-warp ring.
 //
 // One CTA per minibatch node, SPLIT warps.  Warp g handles neighbours
-// g, g+SPLIT, ...: its lane 0 keeps STAGES row copies in flight
-// (cp.async.bulk global -> shared, completion counted on one mbarrier per
-// stage); every lane waits on the stage's barrier, reads its 16-byte
-// vectors of the row from shared memory and does the two FMA passes of the
-// factored gradient (see k_update_phi in ammsb_kernels.cuh for the algebra).
-// All waits are bounded: a wait that runs out sets kErrPipeline, drains the
-// copies this warp still has in flight (also bounded) and the CTA skips its
-// phi write, so a stuck copy cannot hang the GPU.
+// g, g+SPLIT, ...: each of its lanes keeps its own 16-byte pieces of the
+// next STAGES rows in flight (cp.async global -> shared, one commit group
+// per row), waits for the row's group, reads back exactly the pieces it
+// copied and does the two FMA passes of the factored gradient (see
+// k_update_phi in ammsb_kernels.cuh for the algebra).  A lane never reads
+// another lane's pieces of a row, so the ring needs no barrier; the waits are
+// on the lane's own copies, which always complete.  (A variant with one
+// cp.async.bulk copy per row and an mbarrier per slot measured 5% slower:
+// its per-row barrier wait, warp vote, __syncwarp and single-lane issue cost
+// more than four 16-byte copies per lane.)
 #pragma once
 #include "ammsb_kernels.cuh"
 
 namespace ammsb {
 
-enum : int32_t { kErrPipeline = 16 };
-
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Bounded wait: gives up after 200 ms (global timer) or 2^24 polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = global_ns();
-  for (uint32_t it = 0; it < (1u << 16); ++it) {
-    for (int r = 0; r < 256; ++r)
-      if (mbar_try_wait(bar, parity)) return true;
-    if (global_ns() - t0 > 200000000ull) return false;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
 }
 
 // Packed FP32 pairs (Blackwell fma.rn.f32x2): two IEEE round-to-nearest
@@ -127,30 +72,8 @@ struct PairLoad<__nv_bfloat16> {
   }
 };
 
-__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
-  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-// Predicated refill (no branch): when pred, arm `bar` for `bytes` and copy
-// `bytes` from global `src` into shared `dst`, completing on `bar`.  The slot
-// was last touched by the warp's own shared-memory reads, ordered before the
-// copy by the __syncwarp that precedes it; a proxy fence is only needed after
-// generic-proxy writes (the epilogue's A vectors), which the node's first
-// copies follow.
-__device__ __forceinline__ void bulk_copy_g2s_if(bool pred, void* dst, const void* src, uint32_t bytes,
-                                                 uint64_t* bar) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %0, 0;\n\t"
-      "@p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%1], %4;\n\t"
-      "@p cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%2], [%3], %4, [%1];\n\t}" ::"r"(
-          (int)pred),
-      "r"(smem_addr(bar)), "r"(smem_addr(dst)), "l"(src), "r"(bytes)
-      : "memory");
-}
-
 template <typename PiT, int VPL, int SPLIT, int STAGES>
-struct PhiTmaSmem {
+struct PhiRingSmem {
   // BF16 rows keep the node's phi row and normals in shared memory across
   // the rows (two more rows of floats)
   static constexpr bool kStash = sizeof(PiT) == 2;
@@ -158,10 +81,9 @@ struct PhiTmaSmem {
   static_assert(STAGES * sizeof(PiT) >= sizeof(float), "ring slice must hold a row of floats");
   static size_t bytes(int Kp, int n_out) {
     size_t ring = (size_t)SPLIT * STAGES * Kp * sizeof(PiT);
-    size_t bars = (size_t)SPLIT * STAGES * sizeof(uint64_t);
     size_t w = (size_t)(kStash ? 3 : 1) * Kp * sizeof(float);
     size_t misc = (size_t)(4 * SPLIT + 8) * sizeof(float) + (size_t)n_out * sizeof(uint32_t);
-    return ring + bars + w + misc + 128;
+    return ring + w + misc + 128;
   }
 };
 
@@ -215,10 +137,30 @@ __device__ __forceinline__ float4 phi_normals(const Buffers& b, const Stream& rs
 // BF16 rows (STASH) the node's phi row and its normals are read and drawn in
 // the prologue, where they overlap the first copies, and kept in shared
 // memory for the epilogue.
+// The lane's 16-byte pieces of a row (vectors lane + 32 v), copied into the
+// same places of a ring slot by cp.async: a lane only ever reads back the
+// pieces it copied itself.
+template <typename PiT, int VPL, bool FULL>
+__device__ __forceinline__ void copy_row_lane(PiT* dst, const PiT* src, int lane, int nvec) {
+  constexpr int EV = PiTraits<PiT>::kPerVec;
+#pragma unroll
+  for (int v = 0; v < VPL; ++v) {
+    const int vi = lane + 32 * v;
+    if (FULL || vi < nvec)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst + vi * EV)), "l"(src + vi * EV)
+                   : "memory");
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
-__device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffers& b) {
+__device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffers& b) {
   using TR = PiTraits<PiT>;
-  using Smem = PhiTmaSmem<PiT, VPL, SPLIT, STAGES>;
+  using Smem = PhiRingSmem<PiT, VPL, SPLIT, STAGES>;
   constexpr int EV = TR::kPerVec;
   constexpr int EPL = VPL * EV;
   constexpr int NT = SPLIT * 32;
@@ -226,67 +168,40 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
   constexpr bool STASH = Smem::kStash;
   // thread's elements of a row: k0 = 4 * (tid + NT * g) .. k0 + 3, g < NG
   constexpr int NG = (EPL * 32 + 4 * NT - 1) / (4 * NT);
-  static_assert((SPLIT * STAGES) % 2 == 0, "s_w must start on a 16-byte boundary");
-  static_assert(STAGES <= 32, "one lane per first copy");
   extern __shared__ __align__(128) unsigned char s_raw[];
   const int Kp = FULL ? 32 * EPL : m.Kp;
   const int K = m.K, n_out = m.n_out;
   PiT* ring = reinterpret_cast<PiT*>(s_raw);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(ring + (size_t)SPLIT * STAGES * Kp);
-  float* s_w = reinterpret_cast<float*>(bars + SPLIT * STAGES);
+  float* s_w = reinterpret_cast<float*>(ring + (size_t)SPLIT * STAGES * Kp);
   float* s_phi = s_w + Kp;                    // STASH: the node's phi row
   float* s_nz = s_phi + Kp;                   // STASH: its normals
   float* s_red = s_w + (STASH ? 3 : 1) * Kp;  // 4*SPLIT + 8 floats
   uint32_t* s_nb = reinterpret_cast<uint32_t*>(s_red + 4 * SPLIT + 8);
-  __shared__ int s_broken;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n_nodes = b.st->n_nodes;
   const uint32_t step = b.st->step;
   const float eps_t = b.st->eps;
   const PiT* __restrict__ pi = reinterpret_cast<const PiT*>(b.pi);
-  const uint32_t row_bytes = (uint32_t)(Kp * sizeof(PiT));
   const int nvec = Kp / EV;
   const Stream rs{m.seed, m.chain};
 
-  uint64_t* my_bars = bars + warp * STAGES;
   PiT* my_ring = ring + (size_t)warp * STAGES * Kp;
   float* my_A = reinterpret_cast<float*>(my_ring);  // epilogue: this warp's A (Kp floats)
-  if (tid == 0) s_broken = 0;
-  bool dead = false;   // a bounded wait ran out: this warp issues and waits no more
-  bool armed = false;  // this warp's barriers hold valid mbarrier objects
 
   for (int slot = blockIdx.x; slot < n_nodes; slot += gridDim.x) {
     const int32_t i = b.nodes[slot];
     const float* phi_i = b.phi + (int64_t)i * Kp;
     const uint32_t* nbr_g = b.nbr + (int64_t)slot * n_out;
     // rows of this warp: q = warp + SPLIT * t, t < T
-    const int T = (!dead && n_out > warp) ? (n_out - warp + SPLIT - 1) / SPLIT : 0;
-    // lane 0 (re)arms the barriers at phase 0, then lanes 0 .. STAGES-1 each
-    // send one of the first copies, before the node prologue, which they
-    // overlap; the proxy fence orders the previous node's generic accesses
-    // to the ring (its A vectors) before them
-    if (!dead) {
-      if (lane == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-          if (armed) mbar_inval(my_bars + s);
-          mbar_init(my_bars + s, 1);
-        }
-        fence_mbar_init();
-      }
-      armed = true;
-      __syncwarp();
-      const int pre = T < STAGES ? T : STAGES;
-      if (lane < pre) {
-        const uint32_t j = nbr_g[warp + SPLIT * lane] & 0x7fffffffu;
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(my_bars + lane, row_bytes);
-        bulk_copy_g2s(my_ring + (size_t)lane * Kp, pi + (int64_t)j * Kp, row_bytes, my_bars + lane);
-      }
-    }
-    __syncwarp();
-    // ---- node prologue: S = sum phi, s_i = sum pi, w = pi * (beta - eps)
-    float S = 0.f;
+    const int T = (n_out > warp) ? (n_out - warp + SPLIT - 1) / SPLIT : 0;
+    // the first STAGES rows: ids read first, then every lane sends its
+    // pieces, one commit group per row (empty past T), before the node
+    // prologue, which they overlap
+    uint32_t j0[STAGES];
+#pragma unroll
+    for (int t = 0; t < STAGES; ++t) j0[t] = (t < T) ? (nbr_g[warp + SPLIT * t] & 0x7fffffffu) : 0u;
+    // (BF16) the thread's phi elements, loaded before the copies are sent
     float4 ph[STASH ? NG : 1];
     if constexpr (STASH) {
 #pragma unroll
@@ -294,6 +209,15 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
         const int k0 = 4 * (tid + NT * g);
         ph[g] = (k0 < Kp) ? *reinterpret_cast<const float4*>(phi_i + k0) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
+    }
+#pragma unroll
+    for (int t = 0; t < STAGES; ++t) {
+      if (t < T) copy_row_lane<PiT, VPL, FULL>(my_ring + (size_t)t * Kp, pi + (int64_t)j0[t] * Kp, lane, nvec);
+      cp_async_commit();
+    }
+    // ---- node prologue: S = sum phi, s_i = sum pi, w = pi * (beta - eps)
+    float S = 0.f;
+    if constexpr (STASH) {
       for (int q = tid; q < n_out; q += NT) s_nb[q] = nbr_g[q];
 #pragma unroll
       for (int g = 0; g < NG; ++g) {
@@ -375,22 +299,18 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
 #pragma unroll
     for (int u = 0; u < STAGES; ++u) nbw[u] = (u < T) ? s_nb[warp + SPLIT * u] : 0u;
     float Bsum = 0.f;
-    int t_fail = -1;
-    for (int t0 = 0; t0 < T && t_fail < 0; t0 += STAGES) {
-      const uint32_t par = (uint32_t)(t0 / STAGES) & 1u;
+    for (int t0 = 0; t0 < T; t0 += STAGES) {
 #pragma unroll
       for (int u = 0; u < STAGES; ++u) {
         const int t = t0 + u;
         if (t >= T) break;
-        // the lanes agree on the outcome, so a wait that ran out for one
-        // lane sends the whole warp down the same path
-        if (!__all_sync(0xffffffffu, mbar_wait_bounded(my_bars + u, par))) {
-          t_fail = t;
-          break;
-        }
+        // one group per row, so the lane's pieces of row t are in once no
+        // more than the STAGES - 1 later groups are pending
+        cp_async_wait<STAGES - 1>();
         // neighbour word of the row that refills this slot, read early
         const int tn = t + STAGES;
         const uint32_t nxt = (tn < T) ? s_nb[warp + SPLIT * tn] : nbw[u];
+        const bool y = (nbw[u] >> 31) != 0;
         const PiT* row = my_ring + (size_t)u * Kp;
         f32x2 x2[NP];
         load_row_pairs<PiT, VPL, FULL>(row, lane, nvec, x2);
@@ -398,6 +318,11 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
         f32x2 d2[4] = {0ull, 0ull, 0ull, 0ull};
 #pragma unroll
         for (int e = 0; e < NP; ++e) d2[e & 3] = fma_f32x2(w2[e], x2[e], d2[e & 3]);
+        // refill the lane's pieces of slot u (read above, now in registers)
+        // with row t + STAGES
+        if (tn < T) copy_row_lane<PiT, VPL, FULL>(my_ring + (size_t)u * Kp, pi + (int64_t)(nxt & 0x7fffffffu) * Kp, lane, nvec);
+        cp_async_commit();
+        nbw[u] = nxt;
         float D;
         {
           float lo, hi;
@@ -406,7 +331,6 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) D += __shfl_xor_sync(0xffffffffu, D, o);
-        const bool y = (nbw[u] >> 31) != 0;
         const float Ds = y ? D : -D;
         const float P = Ds + (y ? e1si : e0si);
         const float invP = __frcp_rn(P);
@@ -415,24 +339,10 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
         const f32x2 c2 = pack_f32x2(cj, cj);
 #pragma unroll
         for (int e = 0; e < NP; ++e) A2[e] = fma_f32x2(c2, x2[e], A2[e]);
-        __syncwarp();
-        // refill slot u with row t + STAGES once every lane has read row t
-        nbw[u] = nxt;
-        bulk_copy_g2s_if(lane == 0 && tn < T, my_ring + (size_t)u * Kp, pi + (int64_t)(nxt & 0x7fffffffu) * Kp,
-                         row_bytes, my_bars + u);
       }
     }
-    if (t_fail >= 0) {
-      // drain the copies still in flight: rows t_fail .. min(T, t_fail + STAGES) - 1
-      dead = true;
-      const int last = (T < t_fail + STAGES) ? T : t_fail + STAGES;
-      for (int u = t_fail; u < last; ++u)
-        mbar_wait_bounded(my_bars + (u % STAGES), (uint32_t)(u / STAGES) & 1u);
-      if (lane == 0) {
-        atomicOr(&b.gc->err, kErrPipeline);
-        s_broken = 1;
-      }
-    }
+    // every copy of the node is in (the groups after the last row are
+    // empty); the A vectors below reuse the ring
     __syncwarp();
     // ---- publish A (into this warp's own ring slice, now idle) and B
 #pragma unroll
@@ -455,7 +365,6 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
     for (int w2i = 0; w2i < SPLIT; ++w2i) Bt += s_red[2 * SPLIT + w2i];
     const float invS = 1.0f / S;
     const float half_eps = eps_t / 2.0f;
-    const bool write = (s_broken == 0);
     float* phi_w = b.phi + (int64_t)i * Kp;
     float pn[NG][4];
     float Snew = 0.f;
@@ -506,7 +415,7 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
         pn[g][e] = val;
         Snew += val;
       }
-      if (write && k0 < K) {
+      if (k0 < K) {
         if (k0 + 3 < K) {
           *reinterpret_cast<float4*>(phi_w + k0) = make_float4(pn[g][0], pn[g][1], pn[g][2], pn[g][3]);
         } else {
@@ -536,10 +445,7 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
         *reinterpret_cast<float4*>(st + k0) = o;
       }
     }
-    // smem reuse by the next node: every thread's generic accesses to the
-    // ring are ordered before the async proxy's next copies into it
-    fence_proxy_async_smem();
-    __syncthreads();
+    __syncthreads();  // smem reuse by the next node
   }
 }
 // The iteration's node count picks the launch that does the work: the
@@ -549,18 +455,18 @@ __device__ __forceinline__ void update_phi_tma_body(const Model& m, const Buffer
 // 4-warp one gives them, so a node's rows are in flight together.
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
 __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1)
-    k_update_phi_tma(Model m, Buffers b, int n_lo, int n_hi) {
+    k_update_phi_ring(Model m, Buffers b, int n_lo, int n_hi) {
   const int n_nodes = b.st->n_nodes;
   if (n_nodes <= n_lo || n_nodes > n_hi) return;
-  update_phi_tma_body<PiT, VPL, SPLIT, STAGES, FULL>(m, b);
+  update_phi_ring_body<PiT, VPL, SPLIT, STAGES, FULL>(m, b);
 }
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
 __global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1)
-    k_update_phi_tma_chains(const ChainArgs* __restrict__ c, int p, int n_lo, int n_hi) {
+    k_update_phi_ring_chains(const ChainArgs* __restrict__ c, int p, int n_lo, int n_hi) {
   const ChainArgs& a = c[blockIdx.y];
   const int n_nodes = a.b[p].st->n_nodes;
   if (n_nodes <= n_lo || n_nodes > n_hi) return;
-  update_phi_tma_body<PiT, VPL, SPLIT, STAGES, FULL>(a.m, a.b[p]);
+  update_phi_ring_body<PiT, VPL, SPLIT, STAGES, FULL>(a.m, a.b[p]);
 }
 
 }  // namespace ammsb

@@ -88,11 +88,11 @@ class MCMCSamplerStochastic:
         return self.kernel_config()
 
     def kernel_config(self):
-        """(bulk-copy kernel, lanes per node, vectors per lane, sub-groups
+        """(ring kernel, lanes per node, vectors per lane, sub-groups
         per node, ring depth) of update_phi."""
         out = (ctypes.c_int32 * 5)()
         self._check(_native.lib().ammsb_get_kernel_config(self._h, out))
-        return dict(zip(("tma", "lanes", "vectors", "split", "stages"), list(out)))
+        return dict(zip(("ring", "lanes", "vectors", "split", "stages"), list(out)))
 
     def save_checkpoint(self, path):
         """Writes the whole chain (state, counters, running averages, Philox

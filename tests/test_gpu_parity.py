@@ -340,7 +340,7 @@ def wide_net(native_lib):
 @pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
 @pytest.mark.parametrize("K", [1024, 256, 200, 64])
 def test_fed_step_wide_rows(wide_net, K, dtype):
-    """Wide-row kernels: the bulk-copy pipeline (rows of >= 32 vectors; BF16
+    """Wide-row kernels: the shared-memory ring (rows of >= 32 vectors; BF16
     K = 200 has padded rows, partly empty lane vectors) and the sub-warp
     register path (K = 64)."""
     run_fed_case(wide_net, K, 3, dtype, mini_batch_size=64, num_node_sample=40)
@@ -348,22 +348,22 @@ def test_fed_step_wide_rows(wide_net, K, dtype):
 
 @pytest.mark.parametrize("stages", ["3", "6"])
 def test_fed_step_ring_depths(wide_net, stages, monkeypatch):
-    """The bulk-copy kernel at other ring depths (rows per warp not a
+    """The ring kernel at other ring depths (rows per warp not a
     multiple of the depth: 41 neighbours over 4 warps)."""
-    monkeypatch.setenv("AMMSB_PHI_TMA", stages)
+    monkeypatch.setenv("AMMSB_PHI_RING", stages)
     run_fed_case(wide_net, 1024, 9, _native.PI_BF16, mini_batch_size=64, num_node_sample=40)
 
 
 @pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
 @pytest.mark.parametrize("K", [1024, 256])
 def test_fed_step_link_stratum_wide_rows(wide_net, K, dtype):
-    """Few nodes (the link stratum) on the bulk-copy update."""
+    """Few nodes (the link stratum) on the ring update."""
     run_fed_case(wide_net, K, 13, dtype, strategy=1, mini_batch_size=64, num_node_sample=40)
 
 
 def test_fed_step_many_nodes_per_cta(wide_net):
-    """More minibatch nodes than CTAs of one wave, on the bulk-copy kernel:
-    the barriers are re-armed at every node."""
+    """More minibatch nodes than CTAs of one wave, on the ring kernel:
+    every CTA restarts its warps' rings at each node."""
     run_fed_case(wide_net, 256, 7, _native.PI_BF16, strategy=2, mini_batch_size=1400,
                  num_node_sample=20)
 
