@@ -593,6 +593,27 @@ def chains_arm(args):
         s.close()
 
 
+def gather_roofline_arm():
+    """Random whole-row gathers from an 8 GiB table into a shared-memory ring
+    (mcmc_for_ammsb_gb300/csrc/gather_roofline.cu), 16 warps per SM as
+    k_update_phi_ring: one JSON line per row size, then one with the 2 KiB
+    rate as a fraction of the measured copy peak."""
+    from mcmc_for_ammsb_gb300 import build as pkg_build
+    r = subprocess.run([pkg_build.PROBE, "8", "4"], capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stderr)
+        raise SystemExit(r.returncode)
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    for x in lines:
+        print(json.dumps(x))
+    peaks, src = load_peaks()
+    peak = float(peaks.get("hbm_gbs", 0.0))
+    two = [x for x in lines if x["row_bytes"] == 2048]
+    if two and peak:
+        print(json.dumps({"gather_2KiB_GBps": two[0]["GBps"], "copy_peak_GBps": peak, "peak_source": src,
+                          "frac": two[0]["GBps"] / peak}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -623,8 +644,14 @@ def main():
     ap.add_argument("--chains", type=int, default=0,
                     help="run the batching workload with this many chains instead")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--gather-roofline", action="store_true",
+                    help="run the random-row gather probe (the ceiling of update_phi's access "
+                         "pattern) instead of the throughput line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.gather_roofline:
+        gather_roofline_arm()
+        return
     if args.ttp:
         ttp_arm(args)
         return
