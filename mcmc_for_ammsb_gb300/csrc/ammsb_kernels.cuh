@@ -844,7 +844,7 @@ __device__ __forceinline__ void update_phi_body(const Model& m, const Buffers& b
         const float sg_ = y ? 1.f : -1.f;
         const float ej = y ? m.epsilon : 1.0f - m.epsilon;
         const float P = fmaf(sg_, D, ej * s_i);
-        const float invP = __frcp_rn(P);
+        const float invP = rcp_approx(P);
         const float cj = sg_ * invP;
         Bsum += (ej * one_m_si - sg_ * D) * invP;
 #pragma unroll

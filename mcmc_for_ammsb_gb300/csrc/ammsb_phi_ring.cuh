@@ -333,7 +333,7 @@ __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffe
         for (int o = 16; o > 0; o >>= 1) D += __shfl_xor_sync(0xffffffffu, D, o);
         const float Ds = y ? D : -D;
         const float P = Ds + (y ? e1si : e0si);
-        const float invP = __frcp_rn(P);
+        const float invP = rcp_approx(P);
         const float cj = y ? invP : -invP;
         Bsum += ((y ? e1o : e0o) - Ds) * invP;
         const f32x2 c2 = pack_f32x2(cj, cj);
