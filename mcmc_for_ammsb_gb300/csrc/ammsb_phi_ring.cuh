@@ -239,16 +239,17 @@ __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffe
     for (int w = 0; w < SPLIT; ++w) S += s_red[w];
     float si = 0.f;
     if constexpr (STASH) {
+      const float rS = 1.0f / S;  // pi = phi / S as phi * (1/S): within 1 ulp
 #pragma unroll
       for (int g = 0; g < NG; ++g) {
         const int k0 = 4 * (tid + NT * g);
         if (k0 < Kp) {
           const float4 bt = *reinterpret_cast<const float4*>(b.beta + k0);
           float4 p, wv;
-          p.x = __fdiv_rn(ph[g].x, S);
-          p.y = __fdiv_rn(ph[g].y, S);
-          p.z = __fdiv_rn(ph[g].z, S);
-          p.w = __fdiv_rn(ph[g].w, S);
+          p.x = ph[g].x * rS;
+          p.y = ph[g].y * rS;
+          p.z = ph[g].z * rS;
+          p.w = ph[g].w * rS;
           si += p.x;
           si += p.y;
           si += p.z;
@@ -433,15 +434,16 @@ __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffe
 #pragma unroll
     for (int w2i = 0; w2i < SPLIT; ++w2i) Snew += s_red[3 * SPLIT + w2i];
     float* st = b.stage + (int64_t)slot * Kp;
+    const float rSnew = 1.0f / Snew;  // the new pi row as phi * (1/S'): within 1 ulp
 #pragma unroll
     for (int g = 0; g < NG; ++g) {
       const int k0 = 4 * (tid + NT * g);
       if (k0 < Kp) {
         float4 o;
-        o.x = (k0 + 0 < K) ? __fdiv_rn(pn[g][0], Snew) : 0.f;
-        o.y = (k0 + 1 < K) ? __fdiv_rn(pn[g][1], Snew) : 0.f;
-        o.z = (k0 + 2 < K) ? __fdiv_rn(pn[g][2], Snew) : 0.f;
-        o.w = (k0 + 3 < K) ? __fdiv_rn(pn[g][3], Snew) : 0.f;
+        o.x = (k0 + 0 < K) ? pn[g][0] * rSnew : 0.f;
+        o.y = (k0 + 1 < K) ? pn[g][1] * rSnew : 0.f;
+        o.z = (k0 + 2 < K) ? pn[g][2] * rSnew : 0.f;
+        o.w = (k0 + 3 < K) ? pn[g][3] * rSnew : 0.f;
         *reinterpret_cast<float4*>(st + k0) = o;
       }
     }
