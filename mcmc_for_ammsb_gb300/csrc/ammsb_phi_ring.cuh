@@ -127,16 +127,6 @@ __device__ __forceinline__ float4 phi_normals(const Buffers& b, const Stream& rs
   return nz;
 }
 
-// Each warp walks its rows in chunks of STAGES with the ring slot of every
-// row a compile-time constant (the barriers are re-armed from phase 0 at
-// every node), refilling each slot, branch-free, with the row STAGES ahead
-// as soon as the row in it is consumed.  The neighbour word of the row in
-// each slot rides in a register beside the slot.  When FULL the row length
-// is the compile-time 32 * VPL * EV, so row offsets and sizes are constants.
-// A node's first STAGES copies go out from as many lanes at once.  With
-// BF16 rows (STASH) the node's phi row and its normals are read and drawn in
-// the prologue, where they overlap the first copies, and kept in shared
-// memory for the epilogue.
 // The lane's 16-byte pieces of a row (vectors lane + 32 v), copied into the
 // same places of a ring slot by cp.async: a lane only ever reads back the
 // pieces it copied itself.
@@ -157,6 +147,17 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Each warp walks its rows in chunks of STAGES with the ring slot of every
+// row a compile-time constant, refilling each slot with the row STAGES ahead
+// as soon as the row's dot product has taken it into registers; every row
+// commits one group (empty past the node's last row), so
+// cp.async.wait_group STAGES-1 always means "this row is in".  The neighbour
+// word of the row in each slot rides in a register beside the slot.  When
+// FULL the row length is the compile-time 32 * VPL * EV, so row offsets and
+// sizes are constants.  A node's first STAGES rows are sent before its
+// prologue, which they overlap.  With BF16 rows (STASH) the node's phi row
+// and its normals are read and drawn in the prologue and kept in shared
+// memory for the epilogue.
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
 __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffers& b) {
   using TR = PiTraits<PiT>;
