@@ -852,7 +852,7 @@ int ammsb_perplexity(ammsb_handle* h, double* out) {
   if (h->H > 0) {
     CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_ppx<__nv_bfloat16>(h, count) : launch_ppx<float>(h, count));
   }
-  k_ppx_final<<<1, 32, 0, h->stream>>>(h->d_ppx_part, h->H > 0 ? h->ppx_blocks : 0, h->H, h->d_ppx_out);
+  k_ppx_final<<<1, kPpxFinalThreads, 0, h->stream>>>(h->d_ppx_part, h->H > 0 ? h->ppx_blocks : 0, h->H, h->d_ppx_out);
   CK(cudaGetLastError());
   double v = 0.0;
   CK(cudaMemcpyAsync(&v, h->d_ppx_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));

@@ -58,7 +58,7 @@ cudaError_t launch(const Model& m, const void* pi, const float* beta, const int3
                                                    hb, hy, H, ppx, count, scratch);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_ppx_final<<<1, 32, 0, s>>>(scratch, nblk, H, scratch + 2 * kMaxBlocks);
+  k_ppx_final<<<1, kPpxFinalThreads, 0, s>>>(scratch, nblk, H, scratch + 2 * kMaxBlocks);
   return cudaGetLastError();
 }
 
