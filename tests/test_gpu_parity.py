@@ -361,6 +361,14 @@ def test_fed_step_link_stratum_wide_rows(wide_net, K, dtype):
     run_fed_case(wide_net, K, 13, dtype, strategy=1, mini_batch_size=64, num_node_sample=40)
 
 
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+@pytest.mark.parametrize("strategy", [0, 1, 2])
+def test_fed_step_ring_fewer_rows_than_depth(wide_net, dtype, strategy):
+    """Three neighbour rows per node on the ring kernel: warps with fewer rows
+    than the ring depth (empty commit groups) and warps with none."""
+    run_fed_case(wide_net, 1024, 17, dtype, strategy=strategy, mini_batch_size=64, num_node_sample=2)
+
+
 def test_fed_step_many_nodes_per_cta(wide_net):
     """More minibatch nodes than CTAs of one wave, on the ring kernel:
     every CTA restarts its warps' rings at each node."""
