@@ -283,9 +283,11 @@ int ammsb_batch_create(ammsb_handle* const* handles, int32_t n, ammsb_batch** ou
     bt->h.push_back(h);
   }
   bt->device = handles[0]->device;
+  int prio_lo = 0, prio_hi = 0;  // the draws ahead at the higher priority, as for one chain
   if (cudaSetDevice(bt->device) != cudaSuccess ||
+      cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
       cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&bt->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&bt->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaEventCreateWithFlags(&bt->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&bt->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&bt->ev_done, cudaEventDisableTiming) != cudaSuccess) {
@@ -452,7 +454,7 @@ int ammsb_batch_step(ammsb_batch* bt, int64_t n_iters) {
         bt->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
         return AMMSB_E_CUDA;
       }
-      BK(cudaGraphInstantiate(&bt->exec[p], graph, 0));
+      BK(cudaGraphInstantiate(&bt->exec[p], graph, cudaGraphInstantiateFlagUseNodePriority));
       cudaGraphDestroy(graph);
     }
     BK(cudaGraphLaunch(bt->exec[p], bt->stream));

@@ -431,8 +431,13 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
     h->err = "cudaSetDevice failed (no CUDA device?)";
     return bail(AMMSB_E_CUDA);
   }
+  // the draws of the iterations ahead get the higher priority, so their
+  // short launches go in as the update's CTAs retire (graphs keep it: they
+  // are instantiated with node priorities)
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
     h->err = "cudaStreamCreate / cudaEventCreate failed";
@@ -763,7 +768,7 @@ int ammsb_step(ammsb_handle* h, int64_t n_iters) {
           h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
           return AMMSB_E_CUDA;
         }
-        CK(cudaGraphInstantiate(&g, graph, 0));
+        CK(cudaGraphInstantiate(&g, graph, cudaGraphInstantiateFlagUseNodePriority));
         cudaGraphDestroy(graph);
       }
       CK(cudaGraphLaunch(g, h->stream));
