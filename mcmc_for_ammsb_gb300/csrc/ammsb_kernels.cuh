@@ -960,10 +960,18 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
       const int32_t i = b.nodes[slot];
       const float* src = b.stage + (int64_t)slot * Kp;
       PiT* dst = pi + (int64_t)i * Kp;
+      // a vector's EV floats of the staged row (16-byte aligned: Kp is a
+      // multiple of EV) as float4 loads
       for (int vi = lane; vi < nvec; vi += 32) {
         float x[EV];
 #pragma unroll
-        for (int e = 0; e < EV; ++e) x[e] = src[vi * EV + e];
+        for (int e = 0; e < EV; e += 4) {
+          const float4 q = *reinterpret_cast<const float4*>(src + vi * EV + e);
+          x[e] = q.x;
+          x[e + 1] = q.y;
+          x[e + 2] = q.z;
+          x[e + 3] = q.w;
+        }
         *reinterpret_cast<uint4*>(dst + vi * EV) = TR::pack(x);
       }
     }
