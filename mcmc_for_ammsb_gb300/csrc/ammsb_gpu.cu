@@ -237,7 +237,7 @@ int check_device_err(ammsb_handle* h) {
   CK(cudaStreamSynchronize(h->stream));
   if (gc.err) {
     h->err = "device error bits " + std::to_string(gc.err) +
-             " (1 minibatch cap, 2 neighbour cap, 4 capacity, 8 init cap, 16 copy pipeline)";
+             " (1 minibatch cap, 2 neighbour cap, 4 capacity, 8 init cap)";
     if (gc.err & kErrCapacity) return AMMSB_E_CAPACITY;
     return AMMSB_E_SAMPLING;
   }
