@@ -619,6 +619,81 @@ int oracle_step_f32(const oracle_params *p, const oracle_graph *g,
   return rc;
 }
 
+int oracle_step_f32_threads(const oracle_params *p, const oracle_graph *g,
+                            uint32_t step, float *pi, float *phi, float *theta,
+                            float *beta, oracle_mb_info *info, int threads,
+                            int64_t max_edges) {
+  const int32_t K = p->K;
+  if (max_edges <= 0) max_edges = step_max_edges(p, g);
+  int32_t *ea = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
+  int32_t *eb = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_edges);
+  uint8_t *ey = (uint8_t *)malloc((size_t)max_edges);
+  int32_t *nodes = (int32_t *)malloc(sizeof(int32_t) * (size_t)(2 * max_edges + 1));
+  int rc = oracle_sample_minibatch_ex(g, p->strategy, p->mini_batch_size,
+                                      p->max_source, p->num_total_edges, p->seed,
+                                      p->chain, step, ea, eb, ey, (int32_t)max_edges,
+                                      nodes, (int32_t)(2 * max_edges + 1), info);
+  if (rc != 0) {
+    free(ea); free(eb); free(ey); free(nodes);
+    return rc;
+  }
+  const float eps_t = oracle_eps_t(p->a, p->b, p->c, step);
+  const int32_t n_out = (int32_t)p->num_node_sample + 1;
+  const int32_t n_nodes = info->n_nodes;
+  int failed = 0;
+#pragma omp parallel num_threads(threads > 0 ? threads : 1) reduction(| : failed)
+  {
+    int32_t *nb = (int32_t *)malloc(sizeof(int32_t) * (size_t)n_out);
+    uint8_t *ny = (uint8_t *)malloc((size_t)n_out);
+    float *noise = (float *)malloc(sizeof(float) * (size_t)K);
+#pragma omp for schedule(dynamic, 4)
+    for (int32_t s = 0; s < n_nodes; ++s) {
+      const int32_t i = nodes[s];
+      if (oracle_sample_neighbors(g, i, n_out, p->seed, p->chain, step, nb, ny) < 0) {
+        failed = 1;
+        continue;
+      }
+      for (int32_t k = 0; k < K; ++k)
+        noise[k] = oracle_normal(p->seed, p->chain, OR_P_PHI_NOISE, (uint32_t)i,
+                                 step, (uint64_t)k);
+      oracle_update_phi_f32(K, pi, phi + (int64_t)i * K, i, nb, ny, n_out, beta,
+                            p->alpha, p->epsilon, eps_t, p->N, p->num_node_sample,
+                            noise);
+    }
+    free(noise);
+    free(nb);
+    free(ny);
+  }
+  if (failed) rc = -4;
+  if (rc == 0) {
+    for (int32_t s = 0; s < n_nodes; ++s) {
+      const int32_t i = nodes[s];
+      oracle_normalize_f32(K, phi + (int64_t)i * K, pi + (int64_t)i * K);
+    }
+    int32_t *va = (int32_t *)malloc(sizeof(int32_t) * (size_t)(info->n_edges + 1));
+    int32_t *vb = (int32_t *)malloc(sizeof(int32_t) * (size_t)(info->n_edges + 1));
+    for (int32_t e = 0; e < info->n_edges; ++e) {
+      va[e] = nodes[ea[e]];
+      vb[e] = nodes[eb[e]];
+    }
+    float *tn = (float *)malloc(sizeof(float) * 2 * (size_t)K);
+    for (int32_t k = 0; k < 2 * K; ++k)
+      tn[k] = oracle_normal(p->seed, p->chain, OR_P_THETA_NOISE, 0, step,
+                            (uint64_t)k);
+    const float eta[2] = {p->eta0, p->eta1};
+    oracle_update_beta_f32(K, pi, va, vb, ey, info->n_edges, theta, beta, eta,
+                           p->epsilon, eps_t, info->scale, tn, NULL);
+    free(tn);
+    free(va);
+    free(vb);
+  }
+  free(ea);
+  free(eb);
+  free(ey);
+  free(nodes);
+  return rc;
+}
+
 /* The same iteration in double: identical draws (the minibatch, the
  * neighbour sets and the float normals of the Philox spec, widened), double
  * arithmetic throughout, eps_t in double.  The FP64 trajectory reference of

@@ -212,6 +212,43 @@ int oracle_step_f64(const oracle_params *p, const oracle_graph *g,
                     uint32_t step, double *pi, double *phi, double *theta,
                     double *beta, oracle_mb_info *info);
 
+/* The same float iteration with the per-node work (neighbour sets,
+ * update_phi) spread over `threads` host threads (OpenMP), as the
+ * reference's distributed sampler spreads it (distr.cc:1142); results equal
+ * oracle_step_f32's bit for bit (Jacobi: each node writes only its own phi
+ * row).  max_edges: the strategy's minibatch edge capacity, or <= 0 to
+ * compute it from the graph. */
+int oracle_step_f32_threads(const oracle_params *p, const oracle_graph *g,
+                            uint32_t step, float *pi, float *phi, float *theta,
+                            float *beta, oracle_mb_info *info, int threads,
+                            int64_t max_edges);
+
+/* ---- workload inputs (ammsb_oracle_graph.c) -------------------------------*/
+typedef struct {
+  int64_t n, k_true;
+  double zipf_s;
+  int64_t size_min, size_max;
+  double p1, p2, intra_degree, background_frac;
+  uint32_t seed;
+} oracle_gen_params;
+
+/* Planted-community graph as a symmetric CSR with sorted rows; the arrays
+ * are malloc'ed (release with oracle_free).  0 or -1. */
+int oracle_generate_graph(const oracle_gen_params *p, int64_t **row_ptr,
+                          int32_t **col);
+/* p = (ratio * E truncated) / 2: the held-out and the test set each get p
+ * links and p non-links. */
+int64_t oracle_held_out_pairs(int64_t num_edges, double ratio);
+/* Held-out and test sets (2p entries each, caller-allocated). 0 or -1. */
+int oracle_make_held_out(int64_t n, const int64_t *row_ptr, const int32_t *col,
+                         double ratio, uint32_t seed, int32_t *ha, int32_t *hb,
+                         uint8_t *hy, int32_t *ta, int32_t *tb, uint8_t *ty);
+/* A Gamma(1, 1) phi (N x K) and its row-normalised pi, on `threads`
+ * host threads: the starting state of the benchmark's CPU legs. */
+void oracle_init_state_threads(int64_t n, int32_t K, uint32_t seed, float *phi,
+                               float *pi, int threads);
+void oracle_free(void *p);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,7 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libammsb_oracle.so")
-SRC = [os.path.join(HERE, f) for f in ("ammsb_oracle.c", "ammsb_oracle_impl.h", "ammsb_oracle.h")]
+SRC = [os.path.join(HERE, f) for f in ("ammsb_oracle.c", "ammsb_oracle_graph.c",
+                                       "ammsb_oracle_impl.h", "ammsb_oracle.h")]
 
 # stream tags (ammsb_oracle.h)
 P_MB_FLAG, P_MB_NODE, P_MB_CAND, P_NBR, P_PHI_NOISE, P_THETA_NOISE, P_PHI_INIT, P_THETA_INIT = range(1, 9)
@@ -25,7 +26,7 @@ def build(force=False):
             and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in SRC)):
         return LIB
     cmd = ["gcc", "-O2", "-std=c11", "-Wall", "-Wextra", "-ffp-contract=off", "-fPIC", "-shared",
-           "-o", LIB + ".tmp", SRC[0], "-lm"]
+           "-fopenmp", "-o", LIB + ".tmp", SRC[0], SRC[1], "-lm"]
     subprocess.run(cmd, check=True, cwd=HERE)
     os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -82,6 +83,12 @@ def lib():
         L.oracle_perplexity_f64acc.restype = ctypes.c_double
         L.oracle_step_f32.restype = ctypes.c_int
         L.oracle_step_f64.restype = ctypes.c_int
+        L.oracle_step_f32_threads.restype = ctypes.c_int
+        L.oracle_generate_graph.restype = ctypes.c_int
+        L.oracle_held_out_pairs.restype = ctypes.c_int64
+        L.oracle_held_out_pairs.argtypes = [ctypes.c_int64, ctypes.c_double]
+        L.oracle_make_held_out.restype = ctypes.c_int
+        L.oracle_free.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -94,6 +101,67 @@ def philox(ctr, key):
     o = (ctypes.c_uint32 * 4)()
     lib().oracle_philox4x32_10((ctypes.c_uint32 * 4)(*ctr), (ctypes.c_uint32 * 2)(*key), o)
     return list(o)
+
+
+class GenParams(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("k_true", ctypes.c_int64), ("zipf_s", ctypes.c_double),
+                ("size_min", ctypes.c_int64), ("size_max", ctypes.c_int64),
+                ("p1", ctypes.c_double), ("p2", ctypes.c_double),
+                ("intra_degree", ctypes.c_double), ("background_frac", ctypes.c_double),
+                ("seed", ctypes.c_uint32)]
+
+
+class SyntheticNetwork:
+    """A workload's graph and held-out / test sets built by the oracle's own
+    restatement of the generator and the split (ammsb_oracle_graph.c), with
+    the attributes OracleGraph and OracleSampler read.  The CPU legs of the
+    benchmark use it so that they load no library of the product."""
+
+    def __init__(self, row_ptr, col):
+        self.row_ptr = row_ptr
+        self.col = col
+        self.N = int(row_ptr.shape[0] - 1)
+        z = (np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint8))
+        self.held_out, self.test = z, z
+
+    @staticmethod
+    def synthetic(n, k_true, size_min=10, size_max=500, zipf_s=1.5, p1=0.7, p2=0.25,
+                  intra_degree=4.0, background_frac=0.1, seed=0):
+        prm = GenParams(n, k_true, zipf_s, size_min, size_max, p1, p2, intra_degree,
+                        background_frac, seed & 0xffffffff)
+        rp = ctypes.c_void_p()
+        cl = ctypes.c_void_p()
+        if lib().oracle_generate_graph(ctypes.byref(prm), ctypes.byref(rp), ctypes.byref(cl)):
+            raise RuntimeError("oracle graph generation failed")
+        try:
+            row_ptr = np.ctypeslib.as_array(ctypes.cast(rp, ctypes.POINTER(ctypes.c_int64)),
+                                            shape=(n + 1,)).copy()
+            ne = int(row_ptr[-1])
+            col = (np.ctypeslib.as_array(ctypes.cast(cl, ctypes.POINTER(ctypes.c_int32)),
+                                         shape=(ne,)).copy() if ne else np.zeros(0, np.int32))
+        finally:
+            lib().oracle_free(rp)
+            lib().oracle_free(cl)
+        return SyntheticNetwork(row_ptr, col)
+
+    def make_held_out(self, ratio, seed=0):
+        p = lib().oracle_held_out_pairs(self.num_total_edges, ratio)
+        arr = [np.zeros(2 * p, t) for t in (np.int32, np.int32, np.uint8) * 2]
+        rc = lib().oracle_make_held_out(ctypes.c_int64(self.N), _p(self.row_ptr), _p(self.col),
+                                        ctypes.c_double(ratio), ctypes.c_uint32(seed & 0xffffffff),
+                                        *[_p(a) for a in arr])
+        if rc:
+            raise RuntimeError("oracle held-out construction failed")
+        self.held_out = tuple(arr[:3])
+        self.test = tuple(arr[3:])
+        return self
+
+    @property
+    def num_total_edges(self):
+        return int(self.row_ptr[-1]) // 2
+
+    def max_degree(self):
+        return int(np.max(np.diff(self.row_ptr))) if self.N else 0
 
 
 class OracleGraph:
@@ -289,6 +357,33 @@ class OracleSampler:
         rc = lib().oracle_step_f32(ctypes.byref(self.p), ctypes.byref(self.og.g),
                                    ctypes.c_uint32(self.step_count), _p(self.pi), _p(self.phi),
                                    _p(self.theta), _p(self.beta), ctypes.byref(info))
+        if rc != 0:
+            raise RuntimeError("oracle step failed: %d" % rc)
+        self.step_count += 1
+        return info
+
+    def init_state_threads(self, seed, threads):
+        """phi ~ Gamma(1, 1) and pi = phi / sum(phi) for every node, filled
+        on `threads` host threads (oracle_init_state_threads); theta ~
+        Gamma(1, 1) (K x 2)."""
+        N, K = self.N, self.K
+        self.phi = np.empty((N, K), np.float32)
+        self.pi = np.empty((N, K), np.float32)
+        lib().oracle_init_state_threads(ctypes.c_int64(N), ctypes.c_int32(K),
+                                        ctypes.c_uint32(seed & 0xffffffff), _p(self.phi),
+                                        _p(self.pi), ctypes.c_int(threads))
+        rng = np.random.default_rng(seed)
+        self.theta = rng.gamma(1.0, 1.0, (K, 2)).astype(np.float32)
+        self.beta = (self.theta[:, 1] / (self.theta[:, 0] + self.theta[:, 1])).astype(np.float32)
+
+    def step_threads(self, threads, max_edges=0):
+        """The same iteration with the per-node work on `threads` host
+        threads (oracle_step_f32_threads); identical results."""
+        info = MbInfo()
+        rc = lib().oracle_step_f32_threads(
+            ctypes.byref(self.p), ctypes.byref(self.og.g), ctypes.c_uint32(self.step_count),
+            _p(self.pi), _p(self.phi), _p(self.theta), _p(self.beta), ctypes.byref(info),
+            ctypes.c_int(threads), ctypes.c_int64(max_edges))
         if rc != 0:
             raise RuntimeError("oracle step failed: %d" % rc)
         self.step_count += 1

@@ -11,6 +11,11 @@ Rounding differences feed back through the chain (the noise is scaled by
 sqrt(phi), the step reflects at zero), so the gap grows with the
 iterations: on GB300 it was ~7e-4 (FP32) and ~1.2e-3 (BF16) after 500
 iterations of this workload, and ~1.5e-4 on the 100,000-node one.
+
+The mid workload (N=100,000, K=256, num-node-sample 64, minibatch 512)
+runs 500 iterations against the same FP64 restatement, perplexity every
+50: within 2e-3 relative for both pi types, and so within the 1% that the
+trajectory criterion allows.
 """
 import numpy as np
 import pytest
@@ -52,3 +57,39 @@ def test_perplexity_against_fp64_trajectory(native_lib):
         s.close()
         rel = np.abs(np.array(got) - np.array(want)) / np.abs(np.array(want))
         assert rel.max() <= tol, (dt, rel)
+
+
+MID_ITERS, MID_EVERY, MID_TOL = 500, 50, 2e-3
+
+
+def test_mid_perplexity_against_fp64_trajectory(native_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    net, opts = workloads.build("mid")
+    K = 256
+    kw = dict(K=K, num_node_sample=64, mini_batch_size=512, a=0.01, b=1024.0, c=0.55)
+    rng = np.random.default_rng(6)
+    phi = rng.gamma(1.0, 1.0, (net.N, K)).astype(np.float32)
+    theta = rng.gamma(1.0, 1.0, (K, 2))
+    ref = oracle.OracleSampler64(net, K, **{k: v for k, v in kw.items() if k != "K"})
+    ref.set_state(phi, theta)
+    want = []
+    for it in range(MID_ITERS + 1):
+        if it % MID_EVERY == 0:
+            want.append(ref.perplexity())
+        if it < MID_ITERS:
+            ref.step()
+    want = np.array(want)
+    for dt in (_native.PI_F32, _native.PI_BF16):
+        s = MCMCSamplerStochastic(Options(**dict(kw, pi_dtype=dt)), net).set_state(phi, theta)
+        got = []
+        for it in range(0, MID_ITERS + 1, MID_EVERY):
+            got.append(s.cal_perplexity_held_out())
+            if it < MID_ITERS:
+                s.step(MID_EVERY)
+        s.close()
+        rel = np.abs(np.array(got) - want) / np.abs(want)
+        print("\nmid workload, %s pi: max relative perplexity error %.3g over %d iterations"
+              % ("bf16" if dt else "f32", rel.max(), MID_ITERS))
+        assert rel.max() <= MID_TOL, (dt, rel)
