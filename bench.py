@@ -141,102 +141,115 @@ def phi_bytes_per_eval(K, pi_bytes, n_out):
 # ---------------------------------------------------------------------------
 # CPU side: the oracle's restatement of the reference sampler
 # ---------------------------------------------------------------------------
-def cpu_sample(net, opts, seconds, threads, max_steps=None, per_step_nodes=512,
-               pool_rows=1 << 18, seed=0):
-    """Times the reference's per-node work -- neighbour sampling
-    (mcmc_sampler_stochastic.h:87-108) and update_phi (cc:269-313) -- as
-    restated by the oracle, on minibatches of this workload drawn by the
-    sampling spec.  Gathered pi rows come from a pool of `pool_rows` rows
-    (ids mapped modulo the pool) instead of the full N x K array, keeping
-    host memory bounded; the arithmetic per edge evaluation is unchanged.
-    Returns (edge_evals, seconds, steps, nodes)."""
-    import numpy as np
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    from concurrent.futures import ThreadPoolExecutor
+    return oracle
 
-    K = opts.K
-    N = net.N
-    og = oracle.OracleGraph(net)
-    rng = np.random.default_rng(seed)
-    P = min(pool_rows, N)
-    pool = rng.gamma(1.0, 1.0, (P, K)).astype(np.float32)
-    pool /= pool.sum(1, keepdims=True)
-    beta = rng.uniform(0.05, 0.95, K).astype(np.float32)
-    m = opts.mini_batch_size or N // 10
-    nns = opts.num_node_sample or N // 50
-    n_out = nns + 1
-    a = opts.a if opts.a else opts.b ** -opts.c
-    alpha = opts.alpha if opts.alpha else 1.0 / K
-    max_edges = max(m, net.max_degree())
 
-    def node_work(node, step):
-        nb, y = oracle.sample_neighbors(og, node, n_out, 42, 0, step)
-        # local pi over the node and its neighbours (pool rows)
-        rows = np.concatenate([[node], nb]) % P
-        local = pool[rows]
-        lnb = np.arange(1, n_out + 1, dtype=np.int32)
-        phi_i = local[0] * np.float32(K)
-        noise = np.zeros(K, np.float32)
-        oracle.update_phi(K, local, phi_i, 0, lnb, y, beta, alpha, opts.epsilon, 0.01, N, nns,
-                          noise)
-        return n_out
+def cpu_workload(name, strategy=0):
+    """The workload's graph and held-out / test sets built by the oracle's own
+    restatement of the generator and the split (equal to the product's,
+    tests/test_oracle_graph.py), so that the CPU arm loads no product
+    library; returns (network, Options)."""
+    from mcmc_for_ammsb_gb300.options import Options
+    from mcmc_for_ammsb_gb300.workloads import WORKLOADS
+    w = WORKLOADS[name]
+    net = _oracle().SyntheticNetwork.synthetic(**w["gen"])
+    opts = Options(**dict(w["opts"], strategy=strategy))
+    net.make_held_out(opts.held_out_ratio, seed=w["gen"]["seed"])
+    return net, opts
 
-    evals = 0
-    nodes_done = 0
-    steps = 0
+
+def cpu_sampler(net, opts, fill_threads):
+    """The oracle's whole-iteration sampler (float arithmetic in the
+    reference's order) over the workload's full N x K state: phi ~ Gamma(1,
+    1), pi its row normalisation, theta ~ Gamma(1, 1)."""
+    oracle = _oracle()
+    o = oracle.OracleSampler(net, opts.K, strategy=opts.strategy,
+                             mini_batch_size=opts.mini_batch_size or None,
+                             num_node_sample=opts.num_node_sample or None, alpha=opts.alpha,
+                             epsilon=opts.epsilon, eta0=opts.eta0, eta1=opts.eta1, a=opts.a,
+                             b=opts.b, c=opts.c, seed=42)
+    o.init_state_threads(3, fill_threads)
+    # minibatch edge capacity of the strategy (network.cc:188-201)
+    me = max(o.p.mini_batch_size, net.max_degree())
+    if o.p.max_source > 1:
+        me = o.p.mini_batch_size + net.max_degree()
+    if opts.strategy == 3:
+        me = max(me, net.num_total_edges)
+    o.max_edges = me
+    return o
+
+
+def cpu_time(o, threads, max_iters, seconds=None, warmup=0):
+    """Times whole iterations -- minibatch (network.cc:274-421), neighbour
+    sets (mcmc_sampler_stochastic.h:87-108), update_phi (cc:269-313), pi
+    (cc:162-166), update_beta/theta (cc:200-267) -- of the oracle sampler
+    on `threads` host threads, after `warmup` untimed ones; stops after
+    max_iters iterations or, if given, once `seconds` have passed.  Returns
+    (edge evaluations, seconds, iterations, nodes, non-link iterations)."""
+    n_out = o.p.num_node_sample + 1
+    for _ in range(warmup):
+        o.step_threads(threads, o.max_edges)
+    evals = nodes = iters = nonlink = 0
     t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=threads) as ex:
-        step = 1
-        while True:
-            mb = oracle.sample_minibatch(og, opts.strategy, m, net.num_total_edges, 42, 0, step,
-                                         max_edges)
-            nodes = mb["nodes"][:per_step_nodes]
-            evals += sum(ex.map(lambda v: node_work(int(v), step), nodes))
-            nodes_done += len(nodes)
-            steps += 1
-            step += 1
-            el = time.perf_counter() - t0
-            if max_steps is not None:
-                if steps >= max_steps:
-                    break
-            elif el >= seconds:
-                break
-    return evals, time.perf_counter() - t0, steps, nodes_done
+    while iters < max_iters:
+        info = o.step_threads(threads, o.max_edges)
+        evals += info.n_nodes * n_out
+        nodes += info.n_nodes
+        nonlink += info.flag == 0
+        iters += 1
+        if seconds is not None and time.perf_counter() - t0 >= seconds:
+            break
+    return evals, time.perf_counter() - t0, iters, nodes, nonlink
 
 
-def reference_arm(args, net, opts):
+def reference_arm(args):
+    """The reference's CPU sampler on this workload: the oracle's
+    whole-iteration restatement (the compiled reference needs its sources,
+    which only the build container holds) on all host threads, the
+    per-node work spread as the reference's distributed sampler spreads it
+    (distr.cc:1142).  At most 200 iterations are timed so that the run ends
+    in minutes; a 1-thread figure (the reference's sequential build) is
+    taken on the same state."""
     threads = os.cpu_count() or 1
-    # warm-up steps, then timed steps, each a bounded per-iteration sample
-    # (at most 200 iterations are timed, so that the run ends in minutes)
+    from mcmc_for_ammsb_gb300.options import STRATEGIES
+    net, opts = cpu_workload(args.workload, STRATEGIES[args.strategy])
+    o = cpu_sampler(net, opts, threads)
     timed = min(args.steps, 200)
-    cpu_sample(net, opts, 0, threads, max_steps=min(args.warmup, 5),
-               per_step_nodes=args.ref_nodes)
-    ev, secs, steps, nodes = cpu_sample(net, opts, 0, threads, max_steps=timed,
-                                        per_step_nodes=args.ref_nodes, seed=1)
+    ev, secs, iters, nodes, nonlink = cpu_time(o, threads, timed, warmup=min(args.warmup, 5))
     value = ev / secs
-    sample = ("oracle restatement of minibatch + neighbour sampling and update_phi, FP32, on "
-              "up to %d minibatch nodes per iteration of the %s workload (%d iterations timed, "
-              "%d nodes, %d edge evaluations, %d host threads); pi rows from a 2^18-row pool" %
-              (args.ref_nodes, args.workload, steps, nodes, ev, threads))
+    ev1, secs1, iters1, _, nl1 = cpu_time(o, 1, 1000, seconds=args.cpu_seconds)
+    sample = ("oracle restatement of the reference's whole iteration (minibatch, neighbour sets, "
+              "update_phi, pi, update_beta/theta; FP32, reference operation order) on the full "
+              "%d x %d state of the %s workload: %d iterations timed (%d non-link), %d nodes, %d "
+              "edge evaluations, %d host threads (update_phi over nodes); graph and held-out set "
+              "from the oracle's generator" % (net.N, opts.K, args.workload, iters, nonlink, nodes,
+                                               ev, threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(steps, 1),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(iters, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": workload_config(args, net, opts),
+        "data": "synthetic (planted-community generator, seed 0)",
+        "config": workload_config(args.workload, net.N, net.num_total_edges, opts,
+                                  int(net.held_out[0].shape[0])),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
+        "single_thread": {"value": ev1 / secs1, "unit": UNIT, "cores": 1, "iterations": iters1,
+                          "nonlink_iterations": nl1, "seconds": secs1},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
-def workload_config(args, net, opts):
-    return {"workload": args.workload, "N": net.N, "E": net.num_total_edges, "K": opts.K,
+def workload_config(workload, N, E, opts, held_out):
+    """The workload's identity, the same in both arms (the arithmetic type
+    is the line's `dtype`)."""
+    return {"workload": workload, "N": N, "E": E, "K": opts.K,
             "num_node_sample": opts.num_node_sample, "mini_batch_size": opts.mini_batch_size,
-            "strategy": args.strategy, "pi_dtype": args.pi_dtype,
-            "held_out": int(net.held_out[0].shape[0]),
-            "l2": "inputs larger than L2 (pi %.1f GB)" % (net.N * opts.K * (2 if args.pi_dtype == "bf16" else 4) / 1e9)}
+            "strategy": opts.strategy, "held_out": held_out,
+            "l2": "inputs larger than L2 (pi %d x %d)" % (N, opts.K)}
 
 
 # ---------------------------------------------------------------------------
@@ -261,6 +274,9 @@ def ours_arm(args, net, opts, rank, world, local):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    # kernels per iteration: minibatch, neighbour sets, update_phi (the ring
+    # kernel launches its many-node and few-node variants), commit/beta, theta
+    launches_per_iter = 6 if s.kernel_config()["ring"] else 5
     e0, i0 = s.counters()
     clocks = ClockSampler(local)
     clocks.start()
@@ -317,36 +333,50 @@ def ours_arm(args, net, opts, rank, world, local):
     e2e = None
     if rank == 0 and not args.no_e2e:
         interval = opts.interval or 50
+        n_e2e = max(args.steps, args.e2e_steps)
+        s.step(1)  # resumes the draws ahead after the profiled iterations
+        torch.cuda.synchronize()
         ea, _ = s.counters()
         t0 = time.perf_counter()
         n_ppx = 0
         done = 0
-        while done < args.steps:
+        while done < n_e2e:
             if done % interval == 0:
                 s.cal_perplexity_held_out()  # D2H of the perplexity, synchronises
                 n_ppx += 1
-            n = min(interval - done % interval, args.steps - done)
+            n = min(interval - done % interval, n_e2e - done)
             s.step(n)
             done += n
         s.beta  # the iteration's global parameters read back (D2H, synchronises)
         t1 = time.perf_counter()
         eb, _ = s.counters()
         e2e = {"value": (eb - ea) / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": 0,
-               "d2h_bytes_per_step": (8 * n_ppx + 4 * K) / args.steps,
-               "note": "public API loop: step() with held-out perplexity every %d iterations "
-                       "(its D2H read), beta read back at the end, host clock; minibatch and "
-                       "neighbour draws are generated on the device, so an iteration has no "
-                       "host input to copy" % interval}
+               "d2h_bytes_per_step": (8 * n_ppx + 4 * K) / n_e2e, "iterations": n_e2e,
+               "note": "public API loop (what run() does): step() with held-out perplexity "
+                       "every %d iterations (its D2H read), beta read back at the end, host "
+                       "clock, %d iterations; minibatch and neighbour draws are generated on "
+                       "the device, so an iteration has no host input to copy"
+                       % (interval, n_e2e)}
 
+    s.close()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        ev, secs_cpu, steps_cpu, nodes_cpu = cpu_sample(net, opts, args.cpu_seconds, 1,
-                                                        per_step_nodes=args.ref_nodes)
+        o = cpu_sampler(net, opts, os.cpu_count() or 1)
+        ev, secs_cpu, it_cpu, nodes_cpu, nl_cpu = cpu_time(o, 1, 1000, seconds=args.cpu_seconds,
+                                                           warmup=1)
+        del o
         cpu = {"value": ev / secs_cpu, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "oracle restatement (FP32, reference operation order) of neighbour "
-                         "sampling + update_phi on %d minibatch nodes (%d iterations, up to %d "
-                         "nodes each) of this workload, %.1f s on 1 host core" %
-                         (nodes_cpu, steps_cpu, args.ref_nodes, secs_cpu)}
+               "sample": "oracle restatement of the reference's whole iteration (minibatch, "
+                         "neighbour sets, update_phi, pi, update_beta/theta; FP32, reference "
+                         "operation order) on the full %d x %d state of this workload: %d "
+                         "iterations (%d non-link), %d nodes, %.1f s on 1 host core"
+                         % (net.N, K, it_cpu, nl_cpu, nodes_cpu, secs_cpu)}
+
+    ttp = vs_fp64 = None
+    if rank == 0 and world == 1 and args.ttp_iters_line > 0:
+        ttp = ttp_summary(net, opts, args.ttp_iters_line, args.ttp_interval_line)
+    if rank == 0 and world == 1 and not args.no_fp64:
+        vs_fp64 = fp64_summary()
 
     if rank == 0:
         line = {
@@ -355,10 +385,11 @@ def ours_arm(args, net, opts, rank, world, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16-pi/f32" if args.pi_dtype == "bf16" else "f32",
             "data": "synthetic (planted-community generator, seed 0)",
-            "config": dict(workload_config(args, net, opts),
-                           parallelism="replicas" if world > 1 else "single"),
+            "config": workload_config(args.workload, net.N, net.num_total_edges, opts,
+                                      int(net.held_out[0].shape[0])),
+            "parallelism": "replicas" if world > 1 else "single",
             "iterations_per_s": (i1 - i0) / secs if world == 1 else None,
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": launches_per_iter * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved,
                          "peak": peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]),
                          "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0),
@@ -372,22 +403,23 @@ def ours_arm(args, net, opts, rank, world, local):
             "clocks": clk,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "ttp": ttp,
+            "vs_fp64": vs_fp64,
         }
         print(json.dumps(line))
-    s.close()
 
 
 # ---------------------------------------------------------------------------
 # time to perplexity
 # ---------------------------------------------------------------------------
-def _gpu_curve(net, opts_kw, pi_dtype, use_graph, iters, interval):
+def _gpu_curve(net, opts_kw, pi_dtype, use_graph, iters, interval, pipeline=1):
     """Held-out perplexity every `interval` iterations (before the update,
     as run() does) against wall time from the start of the loop; state
     initialisation is outside the clock, as it is outside the reference's
     run() timer."""
     import torch
     from mcmc_for_ammsb_gb300 import MCMCSamplerStochastic, Options, _native
-    o = Options(**dict(opts_kw, pi_dtype=pi_dtype, use_graph=use_graph))
+    o = Options(**dict(opts_kw, pi_dtype=pi_dtype, use_graph=use_graph, pipeline=pipeline))
     s = MCMCSamplerStochastic(o, net).init()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -477,6 +509,99 @@ def _f64_compare(net, kw, iters, interval):
     return out
 
 
+def _grad_vs_fp64():
+    """Error of the FP32 adjoint kernels against the FP64 oracle on the
+    differentiation workload (N=2,000, K=16, phi and theta iid Gamma(100,
+    0.01), 50 nodes x 32 sampled neighbours): the gradient in phi against the
+    oracle's restatement of update_phi's hand-derived gradient
+    (mcmc_sampler_stochastic.cc:274-296), in theta against update_beta's
+    (cc:212-240); largest absolute error over the largest gradient."""
+    import numpy as np
+    import torch
+    oracle = _oracle()
+    from mcmc_for_ammsb_gb300 import workloads
+    from mcmc_for_ammsb_gb300.autograd import edge_log_likelihood
+    net, _ = workloads.build("diff")
+    K, n_nodes, n_out, eps = 16, 50, 32, 1e-7
+    rng = np.random.default_rng(11)
+    phi = rng.gamma(100.0, 0.01, (net.N, K))
+    theta = rng.gamma(100.0, 0.01, (K, 2))
+    og = oracle.OracleGraph(net)
+    nodes = rng.choice(net.N, n_nodes, replace=False).astype(np.int32)
+    drawn = [oracle.sample_neighbors(og, int(v), n_out, 42, 0, 1) for v in nodes]
+    nbrs = np.stack([d[0] for d in drawn])
+    ys = np.stack([d[1] for d in drawn])
+    pi = phi / phi.sum(1, keepdims=True)
+    beta = theta[:, 1] / theta.sum(1)
+    want_phi = np.stack([oracle.phi_grad(K, pi, phi[v], int(v), nbrs[r], ys[r], beta, eps)
+                         for r, v in enumerate(nodes)])
+    ea = np.repeat(nodes, n_out).astype(np.int32)
+    _, _, want_th = oracle.update_beta(K, pi, ea, nbrs.ravel().astype(np.int32), ys.ravel(),
+                                       theta, beta, np.array([1.0, 1.0]), eps, 0.01, 1.0,
+                                       np.zeros((K, 2)), dtype=np.float64)
+    uniq, inv = np.unique(nbrs.ravel(), return_inverse=True)
+    dev = "cuda"
+    ps = torch.tensor(phi[nodes], dtype=torch.float32, device=dev, requires_grad=True)
+    pn = torch.tensor(pi[uniq], dtype=torch.float32, device=dev)
+    th = torch.tensor(theta, dtype=torch.float32, device=dev, requires_grad=True)
+    src = torch.arange(n_nodes, device=dev).repeat_interleave(n_out)
+    L = edge_log_likelihood(ps, pn, th, src, torch.tensor(inv.reshape(-1), device=dev),
+                            torch.tensor(ys.ravel(), dtype=torch.uint8, device=dev), eps)
+    gphi, gth = (t.double().cpu().numpy() for t in torch.autograd.grad(L, (ps, th)))
+    return {"workload": "diff (N=2,000, K=16, 50 nodes x 32 neighbours)", "dtype": "f32",
+            "phi_grad_err": float(np.abs(gphi - want_phi).max() / np.abs(want_phi).max()),
+            "theta_grad_err": float(np.abs(gth - want_th).max() / np.abs(want_th).max())}
+
+
+def fp64_summary():
+    """Errors against the FP64 oracle, stated with every run: held-out
+    perplexity of the FP32 and BF16 device paths over 500 iterations of the
+    small workload (same draws; oracle_step_f64), and the FP32 adjoint's
+    gradient."""
+    from mcmc_for_ammsb_gb300 import workloads
+    net, opts = workloads.build("small")
+    kw = dict(K=32, num_node_sample=32, a=0.01, b=1024.0, c=0.55)
+    f = _f64_compare(net, kw, 500, 50)
+    return {"perplexity": {"workload": "small (N=5,000, K=32), 500 iterations, every 50",
+                           "f32_max_rel_err": f["f32"]["max_rel_err"],
+                           "bf16_max_rel_err": f["bf16"]["max_rel_err"]},
+            "gradient": _grad_vs_fp64()}
+
+
+def ttp_summary(net, opts, iters, interval):
+    """Time to held-out perplexity within 1% of the FP32 plain GPU path's
+    final value (`iters` iterations, perplexity every `interval`), from the
+    same initial state, for
+      f32_plain   FP32 pi, the kernels launched one by one in run()'s loop
+                  order on one stream (draws, then update);
+      f32_graph   FP32 pi with the BF16 sampler's launch design: the
+                  iteration captured in CUDA graphs, the next iterations'
+                  draws on a second stream during the update;
+      bf16_graph  the BF16-pi graph-captured sampler.
+    `speedup` is f32_plain / bf16_graph; `speedup_vs_f32_graph` isolates the
+    BF16 rows (same launch design on both sides)."""
+    from mcmc_for_ammsb_gb300 import _native
+    keys = ("K", "alpha", "eta0", "eta1", "epsilon", "a", "b", "c", "mini_batch_size",
+            "num_node_sample", "strategy", "held_out_ratio")
+    kw = {k: getattr(opts, k) for k in keys}
+    runs = {"f32_plain": _gpu_curve(net, kw, _native.PI_F32, 0, iters, interval, pipeline=0),
+            "f32_graph": _gpu_curve(net, kw, _native.PI_F32, 1, iters, interval),
+            "bf16_graph": _gpu_curve(net, kw, _native.PI_BF16, 1, iters, interval)}
+    target = 1.01 * runs["f32_plain"][-1][2]
+    out = {"target": target, "iterations": iters, "interval": interval}
+    for name, c in runs.items():
+        t, it = _time_to(c, target)
+        out[name] = {"time_to_target_s": t, "iterations_to_target": it,
+                     "final_perplexity": c[-1][2], "wall_s": c[-1][1],
+                     "ms_per_iteration": 1000.0 * c[-1][1] / iters}
+    tb = out["bf16_graph"]["time_to_target_s"]
+    for base, key in (("f32_plain", "speedup"), ("f32_graph", "speedup_vs_f32_graph")):
+        tp = out[base]["time_to_target_s"]
+        out[key] = tp / tb if tp and tb else None
+    out["final_rel_diff"] = abs(runs["bf16_graph"][-1][2] / runs["f32_plain"][-1][2] - 1.0)
+    return out
+
+
 def _time_to(curve, target):
     for it, t, p in curve:
         if p <= target:
@@ -486,8 +611,7 @@ def _time_to(curve, target):
 
 def ttp_arm(args):
     """Time to held-out perplexity within 1% of the FP32 plain GPU path's
-    final value.  `plain` = FP32 pi with every kernel launched one by one
-    (no CUDA graph); the candidate is BF16 pi, graph-captured."""
+    final value, with full curves (see ttp_summary for the three runs)."""
     from mcmc_for_ammsb_gb300 import _native, workloads
     net, opts = workloads.build(args.workload)
     keys = ("K", "alpha", "eta0", "eta1", "epsilon", "a", "b", "c", "mini_batch_size",
@@ -496,7 +620,7 @@ def ttp_arm(args):
     iters = args.ttp_iters
     interval = args.ttp_interval
     runs = {
-        "f32_plain": _gpu_curve(net, kw, _native.PI_F32, 0, iters, interval),
+        "f32_plain": _gpu_curve(net, kw, _native.PI_F32, 0, iters, interval, pipeline=0),
         "f32_graph": _gpu_curve(net, kw, _native.PI_F32, 1, iters, interval),
         "bf16_graph": _gpu_curve(net, kw, _native.PI_BF16, 1, iters, interval),
     }
@@ -599,7 +723,7 @@ def gather_roofline_arm():
     k_update_phi_ring: one JSON line per row size, then one with the 2 KiB
     rate as a fraction of the measured copy peak."""
     from mcmc_for_ammsb_gb300 import build as pkg_build
-    r = subprocess.run([pkg_build.PROBE, "8", "4"], capture_output=True, text=True)
+    r = subprocess.run([pkg_build.build_probe(), "8", "4"], capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stderr)
         raise SystemExit(r.returncode)
@@ -627,9 +751,16 @@ def main():
     ap.add_argument("--pi-dtype", default="bf16", choices=["bf16", "f32"])
     ap.add_argument("--profile-steps", type=int, default=40)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-nodes", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ttp-iters-line", type=int, default=100000,
+                    help="iterations of the time-to-perplexity runs in the throughput line "
+                         "(0: leave them out)")
+    ap.add_argument("--ttp-interval-line", type=int, default=5000)
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="leave out the errors against the FP64 oracle")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2000,
+                    help="iterations of the public-loop (e2e) measurement, at least --steps")
     ap.add_argument("--ttp", action="store_true",
                     help="time to perplexity (FP32 plain vs BF16 graph-captured) instead of "
                          "the throughput line")
@@ -668,10 +799,10 @@ def main():
 
     from mcmc_for_ammsb_gb300 import workloads
     from mcmc_for_ammsb_gb300.options import STRATEGIES
-    net, opts = workloads.build(args.workload, strategy=STRATEGIES[args.strategy])
     if args.impl == "reference":
-        reference_arm(args, net, opts)
+        reference_arm(args)
     else:
+        net, opts = workloads.build(args.workload, strategy=STRATEGIES[args.strategy])
         ours_arm(args, net, opts, rank, world, local)
     if world > 1 and args.impl == "ours":
         import torch.distributed as dist

@@ -82,6 +82,10 @@ typedef struct ammsb_options {
   int32_t device;               /* CUDA device ordinal, default 0 */
   int32_t use_graph;            /* capture the iteration in a CUDA graph (1) */
   int32_t verbose;              /* info lines on stderr like learner.cc:105-120 */
+  int32_t pipeline;             /* 1 (default): the draws of the next two
+                                   iterations run on a second stream during the
+                                   update; 0: run()'s loop order on one stream,
+                                   draws then update (cc:126-170) */
 } ammsb_options;
 
 /* Undirected graph as symmetric CSR: row v lists the neighbours of v in
@@ -249,22 +253,27 @@ int ammsb_load_checkpoint(ammsb_handle *h, const char *path);
  * program whose runtime owns every device allocation, or that must not
  * allocate after start-up) and hold the sampler state in device memory they
  * obtained themselves.  Same kernel and result as ammsb_perplexity, but no
- * handle: pi (row_stride elements per row, 16-byte aligned rows, F32 or
- * BF16), beta, the held-out pairs and the running averages ppx (updated)
+ * handle: pi (n_rows rows of row_stride elements, 16-byte aligned rows, F32
+ * or BF16), beta, the held-out pairs and the running averages ppx (updated)
  * are caller-owned device arrays; *out (host) receives -mean log of the
- * running averages.  Its scratch is a fixed 256 KB __device__ array, so
- * held_count is limited to 4,194,304 (AMMSB_E_CAPACITY beyond).  The array
- * is shared by every call on a device and keeps the last call's contents:
- * calls whose kernels overlap on the GPU race.  The first call on a device
- * looks up the array's address with that device current -- make it before
- * any stream capture.  Runs on `stream` (a cudaStream_t, 0 for the legacy
- * default stream) and synchronises it before returning. */
+ * running averages.  Only the first K elements of a row are read: what the
+ * row padding holds does not matter.  A pair naming a row outside
+ * [0, n_rows) is skipped on the device, before any row is read, and the
+ * call returns AMMSB_E_ARG (the other pairs' running averages are
+ * updated).  Its scratch is a fixed 256 KB __device__ array, so held_count
+ * is limited to 4,194,304 (AMMSB_E_CAPACITY beyond).  The array is shared
+ * by every call on a device and keeps the last call's contents: calls whose
+ * kernels overlap on the GPU race.  The first call on a device looks up the
+ * array's address with that device current.  Runs on `stream` (a
+ * cudaStream_t, 0 for the legacy default stream), copies its result into
+ * host memory and synchronises the stream before returning, so it cannot
+ * be called on a stream that is being captured into a CUDA graph. */
 int ammsb_perplexity_noalloc(const void *pi, int32_t pi_dtype, int64_t K,
-                             int64_t row_stride, const float *beta,
-                             double epsilon, const int32_t *held_a,
-                             const int32_t *held_b, const uint8_t *held_y,
-                             int64_t held_count, float *ppx,
-                             uint64_t average_count, void *stream,
+                             int64_t row_stride, int64_t n_rows,
+                             const float *beta, double epsilon,
+                             const int32_t *held_a, const int32_t *held_b,
+                             const uint8_t *held_y, int64_t held_count,
+                             float *ppx, uint64_t average_count, void *stream,
                              double *out);
 
 /* ------------------------------------------------------------------------ */
@@ -370,6 +379,24 @@ int ammsb_make_held_out(const ammsb_graph_buf *g, double held_out_ratio,
 void ammsb_split_view(const ammsb_split_buf *s, ammsb_edge_set *held_out,
                       ammsb_edge_set *test);
 void ammsb_split_free(ammsb_split_buf *s);
+
+/* Preprocessed networks: Network::save (network.cc:136-145) writes a loaded
+ * network into a directory and Network::Init with input class
+ * "preprocessed" (network.cc:49-65) reads it back instead of the text
+ * graph and the random held-out / test draws.  Here the directory holds
+ * graph.bin (symmetric CSR), held-out.bin (held-out ratio and pairs),
+ * test.bin and aux.bin (N, E, largest degree), an own little-endian
+ * binary layout in place of the reference's gzip'ed sparse-hash dumps.
+ * ammsb_save_preprocessed creates the directory if needed (one level) and
+ * overwrites the files; ammsb_load_preprocessed checks the files' tags and
+ * sizes, the CSR (sorted rows, symmetric, ids in range) and the pairs,
+ * returning AMMSB_E_ARG for anything else, and hands back owned buffers
+ * (ammsb_graph_view / ammsb_split_view read them). */
+int ammsb_save_preprocessed(const ammsb_graph *g, const ammsb_edge_set *held_out,
+                            const ammsb_edge_set *test, double held_out_ratio,
+                            const char *dirname);
+int ammsb_load_preprocessed(const char *dirname, ammsb_graph_buf **graph_out,
+                            ammsb_split_buf **split_out, double *held_out_ratio);
 
 #ifdef __cplusplus
 }

@@ -59,6 +59,7 @@ class AmmsbOptions(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
         ("verbose", ctypes.c_int32),
+        ("pipeline", ctypes.c_int32),
     ]
 
 
@@ -145,8 +146,8 @@ SIGNATURES = [
     ("ammsb_save_checkpoint", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("ammsb_load_checkpoint", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("ammsb_perplexity_noalloc", ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64,
-                                                _P, ctypes.c_double, _P, _P, _P, ctypes.c_int64,
-                                                _P, ctypes.c_uint64, _P, _F64P]),
+                                                ctypes.c_int64, _P, ctypes.c_double, _P, _P, _P,
+                                                ctypes.c_int64, _P, ctypes.c_uint64, _P, _F64P]),
     ("ammsb_edge_loglik_workspace_size", ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int64,
                                                           ctypes.c_int64, ctypes.c_int64]),
     ("ammsb_edge_loglik_forward", ctypes.c_int,
@@ -168,6 +169,13 @@ SIGNATURES = [
                                            ctypes.POINTER(_P)]),
     ("ammsb_split_view", None, [_P, ctypes.POINTER(AmmsbEdgeSet), ctypes.POINTER(AmmsbEdgeSet)]),
     ("ammsb_split_free", None, [_P]),
+    ("ammsb_save_preprocessed", ctypes.c_int, [ctypes.POINTER(AmmsbGraph),
+                                               ctypes.POINTER(AmmsbEdgeSet),
+                                               ctypes.POINTER(AmmsbEdgeSet), ctypes.c_double,
+                                               ctypes.c_char_p]),
+    ("ammsb_load_preprocessed", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P),
+                                               ctypes.POINTER(_P),
+                                               ctypes.POINTER(ctypes.c_double)]),
 ]
 
 

@@ -19,7 +19,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-Wall", "-diag-suppress", "177"]
 SOURCES = ["ammsb_gpu.cu", "ammsb_batch.cu", "ammsb_host.cpp", "ammsb_noalloc.cu", "ammsb_adjoint.cu"]
-# a standalone executable: the random-row gather rate (bench.py --gather-roofline)
+# a standalone measurement executable, not part of the library: the
+# random-row gather rate (bench.py --gather-roofline), built on demand
 PROBE_SRC = "gather_roofline.cu"
 PROBE = os.path.join(HERE, "gather_roofline")
 
@@ -47,7 +48,7 @@ def _deps():
 def build(force=False, verbose=False):
     """Compile libammsb_gpu.so if any source is newer; returns its path."""
     deps = _deps()
-    if not force and _newer(LIB, deps) and _newer(CLI, deps) and _newer(PROBE, deps):
+    if not force and _newer(LIB, deps) and _newer(CLI, deps):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = _nvcc()
@@ -62,17 +63,8 @@ def build(force=False, verbose=False):
             sys.stderr.write(r.stderr)
         return obj
 
-    def compile_probe():
-        cmd = [nvcc] + ARCH + ["-O3", "-std=c++17", os.path.join(CSRC, PROBE_SRC), "-o", PROBE + ".tmp"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (PROBE_SRC, " ".join(cmd), r.stderr))
-        os.replace(PROBE + ".tmp", PROBE)
-
-    with ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as ex:
-        probe = ex.submit(compile_probe)
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-        probe.result()
     tmp = LIB + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -81,6 +73,20 @@ def build(force=False, verbose=False):
     os.replace(tmp, LIB)
     build_cli()
     return LIB
+
+
+def build_probe(force=False):
+    """The gather-rate probe (csrc/gather_roofline.cu), compiled when it is
+    missing or older than its source; returns its path."""
+    src = os.path.join(CSRC, PROBE_SRC)
+    if not force and _newer(PROBE, [src, os.path.abspath(__file__)]):
+        return PROBE
+    cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", src, "-o", PROBE + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (PROBE_SRC, " ".join(cmd), r.stderr))
+    os.replace(PROBE + ".tmp", PROBE)
+    return PROBE
 
 
 CLI = os.path.join(HERE, "ammsb_main")

@@ -82,7 +82,10 @@ cudaError_t launch_phi_t(ammsb_handle* h, const Buffers& b) {
   return cudaGetLastError();
 }
 
-constexpr int kRingSplit = 4;
+#ifndef AMMSB_RING_SPLIT
+#define AMMSB_RING_SPLIT 4
+#endif
+constexpr int kRingSplit = AMMSB_RING_SPLIT;  // warps per node of the many-node ring kernel
 
 template <typename PiT, int VPL, int STAGES, bool FULL>
 cudaError_t launch_phi_ring_t(ammsb_handle* h, const Buffers& b, bool configure) {
@@ -101,11 +104,19 @@ cudaError_t launch_phi_ring_t(ammsb_handle* h, const Buffers& b, bool configure)
     return cudaSuccess;
   }
   if (use_wide) {
-    wide<<<std::min(kRingFewNodes, h->m.max_nodes), kRingSplitWide * 32, smem_w, h->stream>>>(
-        h->m, b, 0, kRingFewNodes);
-    cudaError_t e = cudaGetLastError();
+    // the node count on the device picks the variant that works; the other
+    // returns at once.  They run as parallel branches (a fork onto phi_aux
+    // and a join), so the empty launch does not lengthen the iteration.
+    cudaError_t e = cudaEventRecord(h->ev_phi_fork, h->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->phi_aux, h->ev_phi_fork, 0);
     if (e != cudaSuccess) return e;
+    wide<<<std::min(kRingFewNodes, h->m.max_nodes), kRingSplitWide * 32, smem_w, h->phi_aux>>>(
+        h->m, b, 0, kRingFewNodes);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, kRingFewNodes, INT32_MAX);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(h->ev_phi_join, h->phi_aux)) != cudaSuccess) return e;
+    return cudaStreamWaitEvent(h->stream, h->ev_phi_join, 0);
   } else {
     kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, 0, INT32_MAX);
   }
@@ -170,7 +181,7 @@ cudaError_t launch_ppx(ammsb_handle* h, float count) {
   if (h->cfg.ppx_lpn == L && h->cfg.ppx_vpl == V) {                                            \
     k_perplexity<PiT, L, V><<<nb, 256, 0, h->stream>>>(h->m, pi, h->b.beta, h->d_ha, h->d_hb, \
                                                        h->d_hy, h->H, h->d_ppx, count,        \
-                                                       h->d_ppx_part);                        \
+                                                       h->d_ppx_part, h->m.N, nullptr);       \
     return cudaGetLastError();                                                                 \
   }
   PPX_CASE(1, 1) PPX_CASE(2, 1) PPX_CASE(4, 1) PPX_CASE(8, 1) PPX_CASE(16, 1) PPX_CASE(32, 1)
@@ -190,26 +201,39 @@ cudaError_t launch_normalize(ammsb_handle* h) {
   return cudaGetLastError();
 }
 
-// The iteration's kernels in order; `b` carries the fed-noise pointers when
-// called from ammsb_step_fed (which skips the two sampling kernels).
-cudaError_t launch_update_phase(ammsb_handle* h, const Buffers& b) {
-  cudaError_t e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_phi<__nv_bfloat16>(h, b)
-                                                      : launch_phi<float>(h, b);
-  if (e != cudaSuccess) return e;
-  e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_commit<__nv_bfloat16>(h, b)
-                                          : launch_commit<float>(h, b);
-  if (e != cudaSuccess) return e;
-  k_theta<<<(h->m.K + 31) / 32, 1024, 0, h->stream>>>(h->m, b);
-  return cudaGetLastError();
+// Records `ev` on `s` when timing (ev != nullptr).  Inside a stream
+// capture an external record becomes an event-record node of the graph, so
+// the event is recorded every time the graph runs (a plain record would only
+// mark a dependency of the capture).
+inline cudaError_t mark(cudaEvent_t ev, cudaStream_t s) {
+  return ev ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal) : cudaSuccess;
 }
 
-// Draws of one iteration (minibatch + neighbour sets) into buffer set b.
-cudaError_t launch_sampling_phase(ammsb_handle* h, const Buffers& b, cudaStream_t s) {
+// The iteration's kernels in order; `b` carries the fed-noise pointers when
+// called from ammsb_step_fed (which skips the two sampling kernels).  With
+// `ev`, events are recorded after update_phi, the commit and theta.
+cudaError_t launch_update_phase(ammsb_handle* h, const Buffers& b, const cudaEvent_t* ev = nullptr) {
+  cudaError_t e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_phi<__nv_bfloat16>(h, b)
+                                                      : launch_phi<float>(h, b);
+  if (e != cudaSuccess || (e = mark(ev ? ev[0] : nullptr, h->stream)) != cudaSuccess) return e;
+  e = (h->opt.pi_dtype == AMMSB_PI_BF16) ? launch_commit<__nv_bfloat16>(h, b)
+                                          : launch_commit<float>(h, b);
+  if (e != cudaSuccess || (e = mark(ev ? ev[1] : nullptr, h->stream)) != cudaSuccess) return e;
+  k_theta<<<(h->m.K + 31) / 32, 1024, 0, h->stream>>>(h->m, b);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return mark(ev ? ev[2] : nullptr, h->stream);
+}
+
+// Draws of one iteration (minibatch + neighbour sets) into buffer set b;
+// with `ev`, events after each of the two kernels.
+cudaError_t launch_sampling_phase(ammsb_handle* h, const Buffers& b, cudaStream_t s,
+                                  const cudaEvent_t* ev = nullptr) {
   k_sample_minibatch<<<1, 1024, h->mb_smem, s>>>(h->m, h->g, b, h->mb_smem > 0);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess || (e = mark(ev ? ev[0] : nullptr, s)) != cudaSuccess) return e;
   k_sample_neighbors<8><<<h->nbr_blocks, 256, h->nbr_smem, s>>>(h->m, h->g, b);
-  return cudaGetLastError();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return mark(ev ? ev[1] : nullptr, s);
 }
 
 // `n` (1 or 2) pipelined iterations from ring slot s: the updates of slots
@@ -219,16 +243,135 @@ cudaError_t launch_sampling_phase(ammsb_handle* h, const Buffers& b, cudaStream_
 // the step index, so they can run ahead; taking two iterations per join
 // lets the short updates of link-stratum iterations and the longer draws of
 // the non-link ones even out.
-cudaError_t launch_pipelined(ammsb_handle* h, int s, int n) {
+// With `ev` (run()'s timers): events ev[0] before the first update and
+// ev[1 + 3i ..] after each phase of update i on the update stream, then
+// ev[1 + 3n] before the first draws and ev[2 + 3n + 2i ..] after each of
+// draws i on the draws' stream.
+cudaError_t launch_pipelined(ammsb_handle* h, int s, int n, const cudaEvent_t* ev = nullptr) {
   cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
   if (e != cudaSuccess) return e;
   if ((e = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess) return e;
+  if ((e = mark(ev ? ev[0] : nullptr, h->stream)) != cudaSuccess) return e;
   for (int i = 0; i < n; ++i)
-    if ((e = launch_update_phase(h, h->bufs[(s + i) % kRing])) != cudaSuccess) return e;
+    if ((e = launch_update_phase(h, h->bufs[(s + i) % kRing], ev ? ev + 1 + 3 * i : nullptr)) != cudaSuccess)
+      return e;
+  if ((e = mark(ev ? ev[1 + 3 * n] : nullptr, h->side)) != cudaSuccess) return e;
   for (int i = 0; i < n; ++i)
-    if ((e = launch_sampling_phase(h, h->bufs[(s + 2 + i) % kRing], h->side)) != cudaSuccess) return e;
+    if ((e = launch_sampling_phase(h, h->bufs[(s + 2 + i) % kRing], h->side,
+                                   ev ? ev + 2 + 3 * n + 2 * i : nullptr)) != cudaSuccess)
+      return e;
   if ((e = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess) return e;
   return cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+}
+
+// `n` (1 or 2) iterations from ring slot s in run()'s loop order on the
+// handle's stream, each drawn right before its update (the pipeline
+// option off).  With `ev`: per iteration i, events ev[6i] before the draws,
+// ev[6i + 1], ev[6i + 2] after each draw kernel and ev[6i + 3 ..] after
+// each update phase.
+cudaError_t launch_serial(ammsb_handle* h, int s, int n, const cudaEvent_t* ev = nullptr) {
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n; ++i) {
+    const Buffers& b = h->bufs[(s + i) % kRing];
+    if ((e = mark(ev ? ev[6 * i] : nullptr, h->stream)) != cudaSuccess) return e;
+    if ((e = launch_sampling_phase(h, b, h->stream, ev ? ev + 6 * i + 1 : nullptr)) != cudaSuccess) return e;
+    if ((e = launch_update_phase(h, b, ev ? ev + 6 * i + 3 : nullptr)) != cudaSuccess) return e;
+  }
+  return e;
+}
+
+// Adds the phase durations of a finished timed launch (n iterations from
+// slot s) to run()'s timers; waits for the launch's events.
+int read_phase_events(ammsb_handle* h, int n, int s) {
+  const cudaEvent_t* ev = h->ev_phase[n - 1][s];
+  if (!h->opt.pipeline) {  // launch_serial's layout: 6 events per iteration
+    CK(cudaEventSynchronize(ev[6 * n - 1]));
+    const int order[5] = {ammsb_handle::kTMiniBatch, ammsb_handle::kTNeighbors, ammsb_handle::kTPhi,
+                          ammsb_handle::kTPi, ammsb_handle::kTBeta};
+    for (int i = 0; i < n; ++i)
+      for (int q = 0; q < 5; ++q) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ev[6 * i + q], ev[6 * i + q + 1]));
+        h->timers[order[q]].seconds += ms * 1e-3;
+      }
+    h->timers[ammsb_handle::kTMiniBatch].ticks += (uint64_t)n;
+    h->timers[ammsb_handle::kTPi].ticks += (uint64_t)n;
+    h->timers[ammsb_handle::kTBeta].ticks += (uint64_t)n;
+    return AMMSB_OK;
+  }
+  const cudaEvent_t* sv = ev + 1 + 3 * n;
+  CK(cudaEventSynchronize(ev[3 * n]));
+  CK(cudaEventSynchronize(sv[2 * n]));
+  auto add = [&](int t, cudaEvent_t a, cudaEvent_t b) -> int {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    h->timers[t].seconds += ms * 1e-3;
+    return AMMSB_OK;
+  };
+  for (int i = 0; i < n; ++i) {
+    int rc = add(ammsb_handle::kTPhi, ev[3 * i], ev[3 * i + 1]);
+    if (!rc) rc = add(ammsb_handle::kTPi, ev[3 * i + 1], ev[3 * i + 2]);
+    if (!rc) rc = add(ammsb_handle::kTBeta, ev[3 * i + 2], ev[3 * i + 3]);
+    if (!rc) rc = add(ammsb_handle::kTMiniBatch, sv[2 * i], sv[2 * i + 1]);
+    if (!rc) rc = add(ammsb_handle::kTNeighbors, sv[2 * i + 1], sv[2 * i + 2]);
+    if (rc) return rc;
+  }
+  h->timers[ammsb_handle::kTMiniBatch].ticks += (uint64_t)n;
+  h->timers[ammsb_handle::kTPi].ticks += (uint64_t)n;
+  h->timers[ammsb_handle::kTBeta].ticks += (uint64_t)n;
+  return AMMSB_OK;
+}
+
+// Reads every pending timed launch (all of them, or those up to and
+// including the one that used event set (n, s)).
+int drain_phase_events(ammsb_handle* h, int n = 0, int s = -1) {
+  size_t upto = h->pending.size();
+  if (s >= 0) {
+    upto = 0;
+    for (size_t q = 0; q < h->pending.size(); ++q)
+      if (h->pending[q].n == n && h->pending[q].s == s) upto = q + 1;
+  }
+  for (size_t q = 0; q < upto; ++q) {
+    int rc = read_phase_events(h, h->pending[q].n, h->pending[q].s);
+    if (rc) return rc;
+  }
+  h->pending.erase(h->pending.begin(), h->pending.begin() + (long)upto);
+  return AMMSB_OK;
+}
+
+// Node ticks of sample_neighbor_nodes and update_phi (the reference ticks
+// them once per minibatch node): the edge evaluations the device counted
+// since the last call, over n_out.
+int count_node_ticks(ammsb_handle* h) {
+  DevCounters gc;
+  CK(cudaMemcpyAsync(&gc, h->gc, sizeof(gc), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  const uint64_t nodes = (gc.evals - h->evals_read) / (uint64_t)h->m.n_out;
+  h->timers[ammsb_handle::kTNeighbors].ticks += nodes;
+  h->timers[ammsb_handle::kTPhi].ticks += nodes;
+  h->evals_read = gc.evals;
+  return AMMSB_OK;
+}
+
+// PrintStats (mcmc_sampler_stochastic.cc:185-198) in the reference Timer's
+// tabular layout (timer.cc:18-53): name, total seconds, ticks, microseconds
+// per tick; "<unused>" for a timer that never ticked.
+void print_stats(const ammsb_handle* h) {
+  static const char* names[ammsb_handle::kTimers] = {
+      "  outer", "  perplexity", "  sample_mini_batch", "  nodes_in_mini_batch",
+      "  sample_neighbor_nodes", "  update_phi", "  update_pi", "  update_beta"};
+  std::printf("%-37s%13s%9s%15s\n", "timer", "total (s)", "ticks", "per tick (us)");
+  for (int t = 0; t < ammsb_handle::kTimers; ++t) {
+    const auto& x = h->timers[t];
+    if (x.ticks == 0) {
+      std::printf("%-36s<unused>\n", names[t]);
+    } else {
+      // the total is whole milliseconds, as the reference truncates it
+      std::printf("%-36s %12.3f %8llu %14.3f\n", names[t], std::floor(x.seconds * 1e3) / 1e3,
+                  (unsigned long long)x.ticks, x.seconds * 1e6 / (double)x.ticks);
+    }
+  }
+  std::fflush(stdout);
 }
 
 int check_device_err(ammsb_handle* h) {
@@ -334,6 +477,7 @@ void ammsb_options_default(ammsb_options* o) {
   o->device = 0;
   o->use_graph = 1;
   o->verbose = 0;
+  o->pipeline = 1;
 }
 
 const char* ammsb_create_error(void) { return g_create_error.c_str(); }
@@ -343,15 +487,22 @@ const char* ammsb_last_error(const ammsb_handle* h) { return h ? h->err.c_str() 
 void ammsb_destroy(ammsb_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
-  for (auto& g : h->graph1)
-    if (g) cudaGraphExecDestroy(g);
-  for (auto& g : h->graph2)
-    if (g) cudaGraphExecDestroy(g);
+  for (auto* set : {h->graph1, h->graph2, h->graph1t, h->graph2t})
+    for (int s = 0; s < kRing; ++s)
+      if (set[s]) cudaGraphExecDestroy(set[s]);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->side) cudaStreamSynchronize(h->side);
+  if (h->phi_aux) cudaStreamSynchronize(h->phi_aux);
+  for (auto& per_n : h->ev_phase)
+    for (auto& set : per_n)
+      for (auto& e : set)
+        if (e) cudaEventDestroy(e);
   for (void* p : h->allocs) cudaFree(p);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->ev_phi_fork) cudaEventDestroy(h->ev_phi_fork);
+  if (h->ev_phi_join) cudaEventDestroy(h->ev_phi_join);
+  if (h->phi_aux) cudaStreamDestroy(h->phi_aux);
   if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -438,8 +589,11 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->phi_aux, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_phi_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_phi_join, cudaEventDisableTiming) != cudaSuccess) {
     h->err = "cudaStreamCreate / cudaEventCreate failed";
     return bail(AMMSB_E_CUDA);
   }
@@ -492,7 +646,7 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
     m.nonlink_scale = scale;
     m.link_scale = (float)N;  // network.cc:386-387, max-source 1
   }
-  m.nbb = (int)std::min<int64_t>(256, std::max<int64_t>(1, (max_edges + 3) / 4));
+  m.nbb = (int)std::min<int64_t>(kMaxBetaBlocks, std::max<int64_t>(1, (max_edges + 3) / 4));
   choose_config(h);
   if (h->cfg.vpl > 8) {
     h->err = "K too large for the row kernels";
@@ -749,20 +903,35 @@ int ammsb_step(ammsb_handle* h, int64_t n_iters) {
   CK(cudaSetDevice(h->device));
   if (n_iters == 0) return AMMSB_OK;
   // the draws of the next two iterations, where they are not made yet
-  while (h->ahead < 2) {
+  while (h->opt.pipeline && h->ahead < 2) {
     CK(launch_sampling_phase(h, h->bufs[(h->slot + h->ahead) % kRing], h->stream));
     ++h->ahead;
   }
+  auto launch = [&](int s, int n, const cudaEvent_t* ev) {
+    return h->opt.pipeline ? launch_pipelined(h, s, n, ev) : launch_serial(h, s, n, ev);
+  };
   int64_t left = n_iters;
   while (left > 0) {
     const int n = left >= 2 ? 2 : 1;
     const int s = h->slot;
+    // run()'s timers: the launch records events between the phases; the
+    // events of an earlier launch with the same event set are read first
+    const cudaEvent_t* ev = nullptr;
+    if (h->timing) {
+      cudaEvent_t* set = h->ev_phase[n - 1][s];
+      if (!set[0])
+        for (int q = 0; q < 12; ++q) CK(cudaEventCreate(&set[q]));
+      int rc = drain_phase_events(h, n, s);
+      if (rc) return rc;
+      ev = set;
+    }
     if (h->opt.use_graph) {
-      cudaGraphExec_t& g = (n == 2) ? h->graph2[s] : h->graph1[s];
+      cudaGraphExec_t& g = h->timing ? ((n == 2) ? h->graph2t[s] : h->graph1t[s])
+                                     : ((n == 2) ? h->graph2[s] : h->graph1[s]);
       if (!g) {
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = launch_pipelined(h, s, n);
+        cudaError_t e = launch(s, n, ev);
         cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
         if (e != cudaSuccess || e2 != cudaSuccess) {
           h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
@@ -773,8 +942,9 @@ int ammsb_step(ammsb_handle* h, int64_t n_iters) {
       }
       CK(cudaGraphLaunch(g, h->stream));
     } else {
-      CK(launch_pipelined(h, s, n));
+      CK(launch(s, n, ev));
     }
+    if (h->timing) h->pending.push_back({n, s});
     h->last = (s + n - 1) % kRing;
     h->slot = (s + n) % kRing;
     left -= n;
@@ -874,6 +1044,7 @@ int ammsb_run(ammsb_handle* h, double* last) {
     int rc = ammsb_init_state(h);
     if (rc) return rc;
   }
+  using clk = std::chrono::steady_clock;
   const auto t0 = std::chrono::system_clock::now();
   double ppx = 0.0;
   auto converged = [&]() {  // learner.cc:130-136
@@ -882,10 +1053,44 @@ int ammsb_run(ammsb_handle* h, double* last) {
     return std::fabs(h->ppx_history[n - 1] - h->ppx_history[n - 2]) / h->ppx_history[n - 2] <=
            h->opt.convergence_threshold;
   };
+  // the timers (cc:95-102) start from zero and time this run
+  for (auto& t : h->timers) t = ammsb_handle::Timer{};
+  h->pending.clear();
+  {
+    int rc = count_node_ticks(h);  // node ticks count from here
+    if (rc) return rc;
+    h->timers[ammsb_handle::kTNeighbors].ticks = h->timers[ammsb_handle::kTPhi].ticks = 0;
+  }
+  h->timing = true;
+  auto finish = [&](int rc) {
+    h->timing = false;
+    return rc;
+  };
+  const uint64_t stats_every = (uint64_t)h->opt.stats_print_interval;
+  const uint64_t first_step = h->step_count;
+  auto outer_start = clk::now();
+  // the outer timer: wall time of the iterations (perplexity included), one
+  // tick per iteration; brought up to date at every stats print
+  auto stats = [&]() -> int {
+    int rc = drain_phase_events(h);
+    if (!rc) rc = count_node_ticks(h);
+    if (rc) return rc;
+    const auto now = clk::now();
+    h->timers[ammsb_handle::kTOuter].seconds += std::chrono::duration<double>(now - outer_start).count();
+    h->timers[ammsb_handle::kTOuter].ticks = h->step_count - first_step;
+    outer_start = now;
+    print_stats(h);
+    outer_start = clk::now();  // printing is not an iteration's time
+    return AMMSB_OK;
+  };
   while (h->step_count < (uint64_t)h->opt.max_iteration && !converged()) {
     if ((h->step_count - 1) % (uint64_t)h->opt.interval == 0) {
+      const auto p0 = clk::now();
       int rc = ammsb_perplexity(h, &ppx);
-      if (rc) return rc;
+      if (rc) return finish(rc);
+      h->timers[ammsb_handle::kTPerplexity].seconds +=
+          std::chrono::duration<double>(clk::now() - p0).count();
+      h->timers[ammsb_handle::kTPerplexity].ticks += 1;
       const double secs =
           std::chrono::duration<double>(std::chrono::system_clock::now() - t0).count();
       std::printf("average_count is: %llu step count: %llu time: %.3f perplexity for hold out set: %.12f\n",
@@ -893,18 +1098,21 @@ int ammsb_run(ammsb_handle* h, double* last) {
       std::fflush(stdout);
       h->ppx_history.push_back(ppx);
     }
-    // run up to the next perplexity point
+    // run up to the next perplexity point or stats print, whichever is first
     const uint64_t interval = (uint64_t)h->opt.interval;
     uint64_t until = ((h->step_count - 1) / interval + 1) * interval + 1;
+    until = std::min<uint64_t>(until, (h->step_count / stats_every + 1) * stats_every);
     until = std::min<uint64_t>(until, (uint64_t)h->opt.max_iteration);
     const int64_t n = (int64_t)(until - h->step_count);
     int rc = ammsb_step(h, std::max<int64_t>(n, 1));
-    if (rc) return rc;
+    if (rc) return finish(rc);
+    if (h->step_count % stats_every == 0 && (rc = stats()) != AMMSB_OK) return finish(rc);  // cc:177-179
   }
   int rc = check_device_err(h);
-  if (rc) return rc;
+  if (!rc) rc = stats();  // cc:182
+  if (rc) return finish(rc);
   if (last) *last = ppx;
-  return AMMSB_OK;
+  return finish(AMMSB_OK);
 }
 
 int ammsb_get_pi(ammsb_handle* h, float* dst) {

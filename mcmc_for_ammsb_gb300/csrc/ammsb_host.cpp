@@ -9,11 +9,15 @@
 // the graph is a symmetric CSR with sorted rows -- the layout the GPU binary
 // searches -- and every random choice comes from the Philox streams of
 // ammsb_rng.h so the result does not depend on hash-table iteration order.
+#include <errno.h>
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <unordered_set>
@@ -371,5 +375,161 @@ void ammsb_split_view(const ammsb_split_buf* s, ammsb_edge_set* held_out,
 }
 
 void ammsb_split_free(ammsb_split_buf* s) { delete s; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Preprocessed networks: the reference saves a loaded network (graph,
+// held-out set with its ratio and size, test set, auxiliary degree data)
+// into a directory (network.cc:88-145) and reloads it with input class
+// "preprocessed" (network.cc:49-65) instead of reading text and drawing the
+// sets again.  Here the directory holds four little-endian binary files:
+//   graph.bin     "AMMSBG01", n, nnz (= 2E), row_ptr[n + 1] (int64), col[nnz] (int32)
+//   held-out.bin  "AMMSBH01", held_out_ratio (double), count, a[], b[] (int32), y[] (u8)
+//   test.bin      "AMMSBT01", count, a[], b[], y[]
+//   aux.bin       "AMMSBA01", n, E, largest degree
+// Every count is an int64.  The loader checks the tags, the sizes (no
+// short or overlong file), the CSR (row_ptr from 0 up to nnz, columns in
+// range, each row sorted without repeats and symmetric in count) and the
+// pairs (vertices in range, a != b).
+namespace {
+
+bool put(FILE* f, const void* p, size_t bytes) { return bytes == 0 || std::fwrite(p, 1, bytes, f) == bytes; }
+bool get(FILE* f, void* p, size_t bytes) { return bytes == 0 || std::fread(p, 1, bytes, f) == bytes; }
+
+bool at_eof(FILE* f) {
+  unsigned char c;
+  return std::fread(&c, 1, 1, f) == 0;
+}
+
+struct File {
+  FILE* f;
+  explicit File(const std::string& path, const char* mode) : f(std::fopen(path.c_str(), mode)) {}
+  ~File() {
+    if (f) std::fclose(f);
+  }
+  bool close() {
+    const bool ok = f && std::fclose(f) == 0;
+    f = nullptr;
+    return ok;
+  }
+};
+
+bool write_pairs(FILE* f, const ammsb_edge_set* s) {
+  const int64_t c = s ? s->count : 0;
+  return put(f, &c, 8) && (c == 0 || (put(f, s->a, 4 * (size_t)c) && put(f, s->b, 4 * (size_t)c) &&
+                                      put(f, s->y, (size_t)c)));
+}
+
+bool read_pairs(FILE* f, int64_t n, std::vector<int32_t>& a, std::vector<int32_t>& b,
+                std::vector<uint8_t>& y) {
+  int64_t c = 0;
+  if (!get(f, &c, 8) || c < 0 || c > (int64_t)1 << 40) return false;
+  a.resize((size_t)c);
+  b.resize((size_t)c);
+  y.resize((size_t)c);
+  if (!get(f, a.data(), 4 * (size_t)c) || !get(f, b.data(), 4 * (size_t)c) || !get(f, y.data(), (size_t)c))
+    return false;
+  for (int64_t q = 0; q < c; ++q)
+    if (a[q] < 0 || b[q] < 0 || a[q] >= n || b[q] >= n || a[q] == b[q] || y[q] > 1) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ammsb_save_preprocessed(const ammsb_graph* g, const ammsb_edge_set* held_out,
+                            const ammsb_edge_set* test, double held_out_ratio, const char* dirname) {
+  if (!g || !dirname || g->n < 1 || !g->row_ptr || (g->row_ptr[g->n] > 0 && !g->col))
+    return AMMSB_E_ARG;
+  if (mkdir(dirname, 0777) != 0 && errno != EEXIST) return AMMSB_E_ARG;
+  const std::string dir(dirname);
+  const int64_t n = g->n, nnz = g->row_ptr[n];
+  {
+    File f(dir + "/graph.bin", "wb");
+    if (!f.f || !put(f.f, "AMMSBG01", 8) || !put(f.f, &n, 8) || !put(f.f, &nnz, 8) ||
+        !put(f.f, g->row_ptr, 8 * (size_t)(n + 1)) || !put(f.f, g->col, 4 * (size_t)nnz) || !f.close())
+      return AMMSB_E_ARG;
+  }
+  {
+    File f(dir + "/held-out.bin", "wb");
+    if (!f.f || !put(f.f, "AMMSBH01", 8) || !put(f.f, &held_out_ratio, 8) ||
+        !write_pairs(f.f, held_out) || !f.close())
+      return AMMSB_E_ARG;
+  }
+  {
+    File f(dir + "/test.bin", "wb");
+    if (!f.f || !put(f.f, "AMMSBT01", 8) || !write_pairs(f.f, test) || !f.close()) return AMMSB_E_ARG;
+  }
+  int64_t maxdeg = 0;
+  for (int64_t v = 0; v < n; ++v) maxdeg = std::max(maxdeg, g->row_ptr[v + 1] - g->row_ptr[v]);
+  const int64_t E = nnz / 2;
+  File f(dir + "/aux.bin", "wb");
+  if (!f.f || !put(f.f, "AMMSBA01", 8) || !put(f.f, &n, 8) || !put(f.f, &E, 8) || !put(f.f, &maxdeg, 8) ||
+      !f.close())
+    return AMMSB_E_ARG;
+  return AMMSB_OK;
+}
+
+int ammsb_load_preprocessed(const char* dirname, ammsb_graph_buf** graph_out,
+                            ammsb_split_buf** split_out, double* held_out_ratio) {
+  if (!dirname || !graph_out || !split_out) return AMMSB_E_ARG;
+  const std::string dir(dirname);
+  char tag[8];
+  auto g = std::make_unique<ammsb_graph_buf>();
+  {
+    File f(dir + "/graph.bin", "rb");
+    int64_t n = 0, nnz = 0;
+    if (!f.f || !get(f.f, tag, 8) || std::memcmp(tag, "AMMSBG01", 8) != 0 || !get(f.f, &n, 8) ||
+        !get(f.f, &nnz, 8) || n < 1 || n > (int64_t)INT32_MAX || nnz < 0 || nnz % 2 != 0 ||
+        nnz > (int64_t)1 << 40)
+      return AMMSB_E_ARG;
+    g->n = n;
+    g->row_ptr.resize((size_t)n + 1);
+    g->col.resize((size_t)nnz);
+    if (!get(f.f, g->row_ptr.data(), 8 * (size_t)(n + 1)) || !get(f.f, g->col.data(), 4 * (size_t)nnz) ||
+        !at_eof(f.f))
+      return AMMSB_E_ARG;
+    if (g->row_ptr[0] != 0 || g->row_ptr[n] != nnz) return AMMSB_E_ARG;
+    for (int64_t v = 0; v < n; ++v) {
+      const int64_t lo = g->row_ptr[v], hi = g->row_ptr[v + 1];
+      if (hi < lo || hi > nnz) return AMMSB_E_ARG;
+      for (int64_t q = lo; q < hi; ++q)
+        if (g->col[q] < 0 || g->col[q] >= n || g->col[q] == v || (q > lo && g->col[q] <= g->col[q - 1]))
+          return AMMSB_E_ARG;
+    }
+  }
+  auto s = std::make_unique<ammsb_split_buf>();
+  double ratio = 0.0;
+  {
+    File f(dir + "/held-out.bin", "rb");
+    if (!f.f || !get(f.f, tag, 8) || std::memcmp(tag, "AMMSBH01", 8) != 0 || !get(f.f, &ratio, 8) ||
+        !(ratio >= 0.0 && ratio < 1.0) || !read_pairs(f.f, g->n, s->ha, s->hb, s->hy) || !at_eof(f.f))
+      return AMMSB_E_ARG;
+  }
+  {
+    File f(dir + "/test.bin", "rb");
+    if (!f.f || !get(f.f, tag, 8) || std::memcmp(tag, "AMMSBT01", 8) != 0 ||
+        !read_pairs(f.f, g->n, s->ta, s->tb, s->ty) || !at_eof(f.f))
+      return AMMSB_E_ARG;
+  }
+  {
+    File f(dir + "/aux.bin", "rb");
+    int64_t n = 0, E = 0, maxdeg = 0;
+    if (!f.f || !get(f.f, tag, 8) || std::memcmp(tag, "AMMSBA01", 8) != 0 || !get(f.f, &n, 8) ||
+        !get(f.f, &E, 8) || !get(f.f, &maxdeg, 8) || !at_eof(f.f) || n != g->n ||
+        E != (int64_t)g->col.size() / 2)
+      return AMMSB_E_ARG;
+  }
+  // a symmetric graph: every entry (v, u) has its (u, v)
+  for (int64_t v = 0; v < g->n; ++v)
+    for (int64_t q = g->row_ptr[v]; q < g->row_ptr[v + 1]; ++q)
+      if (!has_edge(g.get(), g->col[q], (int32_t)v)) return AMMSB_E_ARG;
+  if (held_out_ratio) *held_out_ratio = ratio;
+  *graph_out = g.release();
+  *split_out = s.release();
+  return AMMSB_OK;
+}
 
 }  // extern "C"

@@ -31,6 +31,10 @@ struct ammsb_handle {
   cudaStream_t stream = nullptr;  // the handle's stream: updates, perplexity, copies
   cudaStream_t side = nullptr;    // draws of the next iteration, overlapped with the update
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // the few-node update_phi variant runs beside the many-node one (only one
+  // of them has work in an iteration), so the idle launch is off the path
+  cudaStream_t phi_aux = nullptr;
+  cudaEvent_t ev_phi_fork = nullptr, ev_phi_join = nullptr;
   Model m{};
   DevGraph g{};
   Buffers b{};        // shared state pointers (bufs[s] add the minibatch buffers)
@@ -65,6 +69,25 @@ struct ammsb_handle {
   // captured iterations per ring slot: one iteration, and two iterations
   // with the draws of the following two made alongside
   cudaGraphExec_t graph1[kRing] = {}, graph2[kRing] = {};
+  // run()'s per-phase timers (mcmc_sampler_stochastic.cc:93-102), printed
+  // as PrintStats does (cc:185-198): wall time and ticks per timer
+  struct Timer {
+    double seconds = 0.0;
+    uint64_t ticks = 0;
+  };
+  enum { kTOuter, kTPerplexity, kTMiniBatch, kTNodes, kTNeighbors, kTPhi, kTPi, kTBeta, kTimers };
+  Timer timers[kTimers];
+  bool timing = false;  // run() launches the timed captures below
+  // the same iterations with CUDA events between the phases: per launch of
+  // n iterations, 1 + 3n events on the update stream, then 1 + 2n on the
+  // draws' stream; one event set per (n, slot)
+  cudaGraphExec_t graph1t[kRing] = {}, graph2t[kRing] = {};
+  cudaEvent_t ev_phase[2][kRing][12] = {};
+  struct Pending {
+    int n, s;
+  };
+  std::vector<Pending> pending;  // timed launches whose events are not read yet
+  uint64_t evals_read = 0;       // edge evaluations counted into the timers' ticks
   std::string err;
 };
 

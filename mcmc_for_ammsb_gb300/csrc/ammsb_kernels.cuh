@@ -18,6 +18,14 @@
 
 namespace ammsb {
 
+// Upper bound of Model::nbb, the blocks of k_commit_beta that write beta
+// gradient partials (k_theta reads them back, kMaxBetaBlocks / 32 per warp).
+#ifndef AMMSB_MAX_BETA_BLOCKS
+#define AMMSB_MAX_BETA_BLOCKS 256
+#endif
+constexpr int kMaxBetaBlocks = AMMSB_MAX_BETA_BLOCKS;
+static_assert(kMaxBetaBlocks % 256 == 0, "k_theta reads the partials in chunks of 8 per warp");
+
 struct Model {
   int32_t K;      // communities
   int32_t Kp;     // row stride in elements (K rounded up to 16 bytes)
@@ -32,7 +40,7 @@ struct Model {
   int32_t mini_batch_size;
   int32_t strategy;
   float nonlink_scale, link_scale;
-  int32_t nbb;    // beta partial blocks
+  int32_t nbb;    // beta partial blocks (at most kMaxBetaBlocks)
   int32_t nbr_set_cap;  // per-warp accepted-neighbour set capacity (power of two)
   int32_t max_source;   // sampler.max-source (link stratum)
   int32_t full_set;     // random-edge: the minibatch is the whole training set
@@ -1070,16 +1078,37 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
   const int k = blockIdx.x * 32 + lane;
   const int Kp = m.Kp;
   const int active = min(m.nbb, (b.st->n_edges + 3) / 4);  // blocks that saw edges
+  // the step's scalars and this k's theta and beta, fetched now so that their
+  // latency overlaps the partial sums
+  const uint32_t step = b.st->step;
+  const double eps_t = (double)b.st->eps;
+  const double scale = (double)b.st->scale;
+  const bool kin = k < m.K;
+  const double th0 = kin ? b.theta[2 * k] : 1.0, th1 = kin ? b.theta[2 * k + 1] : 1.0;
+  const double bt = kin ? (double)b.beta[k] : 0.0;
+  // the warp's partials (blocks warp, warp + 32, ...) loaded eight at a
+  // time, each eight together, then added in block order
   float r0 = 0.f, c0 = 0.f, r1 = 0.f, c1 = 0.f;
-  if (k < m.K) {
-    for (int bb = warp; bb < active; bb += 32) {
+  for (int base = warp; base < active; base += 32 * 8) {
+    float p0v[8], p1v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int bb = base + 32 * q;
+      const bool on = kin && bb < active;
       const float* p0 = b.beta_part + (int64_t)bb * 2 * Kp + k;
-      const float y0 = p0[0] - c0, y1 = p0[Kp] - c1;
-      const float t0 = r0 + y0, t1 = r1 + y1;
-      c0 = (t0 - r0) - y0;
-      c1 = (t1 - r1) - y1;
-      r0 = t0;
-      r1 = t1;
+      p0v[q] = on ? p0[0] : 0.f;
+      p1v[q] = on ? p0[Kp] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (base + 32 * q < active) {
+        const float y0 = p0v[q] - c0, y1 = p1v[q] - c1;
+        const float t0 = r0 + y0, t1 = r1 + y1;
+        c0 = (t0 - r0) - y0;
+        c1 = (t1 - r1) - y1;
+        r0 = t0;
+        r1 = t1;
+      }
     }
   }
   s_r0[warp][lane] = r0;
@@ -1100,16 +1129,11 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
     a1 = t1;
   }
   const double R0 = (double)a0 - (double)e0, R1 = (double)a1 - (double)e1;
-  const uint32_t step = b.st->step;
-  const double eps_t = (double)b.st->eps;
-  const double scale = (double)b.st->scale;
   if (k == 0) {  // the iteration's edge evaluations, counted once it is applied
     b.gc->evals += (unsigned long long)b.st->n_nodes * (unsigned long long)m.n_out;
     b.gc->iters += 1ull;
   }
-  const double th0 = b.theta[2 * k], th1 = b.theta[2 * k + 1];
   const double ts_inv = 1.0 / (th0 + th1);
-  const double bt = (double)b.beta[k];
   const double G0 = bt * R1 * (-ts_inv) + (1.0 - bt) * R0 * (1.0 / th0 - ts_inv);
   const double G1 = bt * R1 * (1.0 / th1 - ts_inv) + (1.0 - bt) * R0 * (-ts_inv);
   const Stream rs{m.seed, m.chain};
@@ -1147,14 +1171,17 @@ __global__ void __launch_bounds__(256) k_perplexity(Model m, const PiT* __restri
                                                     const int32_t* __restrict__ hb,
                                                     const uint8_t* __restrict__ hy, int64_t H,
                                                     float* __restrict__ ppx, float count,
-                                                    double* __restrict__ part) {
+                                                    double* __restrict__ part, int64_t n_rows,
+                                                    unsigned int* __restrict__ bad) {
   using TR = PiTraits<PiT>;
   constexpr int EV = TR::kPerVec;
   constexpr int EPL = VPL * EV;
   constexpr int GPB = 256 / LPN;
   const int tid = threadIdx.x, grp = tid / LPN, l = tid % LPN, lane = tid & 31;
   const uint32_t gmask = group_mask<LPN>(lane);
-  const int Kp = m.Kp, K = m.K, nvec = Kp / EV;
+  // rows are Kp apart; only the vectors that hold the K values are read,
+  // and elements past K (row padding) take no part in either sum
+  const int Kp = m.Kp, K = m.K, nvec = (K + EV - 1) / EV;
   float bt[EPL];
 #pragma unroll
   for (int v = 0; v < VPL; ++v)
@@ -1165,8 +1192,14 @@ __global__ void __launch_bounds__(256) k_perplexity(Model m, const PiT* __restri
     }
   double sum = 0.0, comp = 0.0;
   for (int64_t ed = (int64_t)blockIdx.x * GPB + grp; ed < H; ed += (int64_t)gridDim.x * GPB) {
-    const PiT* ra = pi + (int64_t)ha[ed] * Kp;
-    const PiT* rb = pi + (int64_t)hb[ed] * Kp;
+    const int32_t a = ha[ed], b = hb[ed];
+    // a pair naming a row outside pi is skipped (no row is read) and flagged
+    if ((uint64_t)(int64_t)a >= (uint64_t)n_rows || (uint64_t)(int64_t)b >= (uint64_t)n_rows) {
+      if (l == 0 && bad) atomicOr(bad, 1u);
+      continue;
+    }
+    const PiT* ra = pi + (int64_t)a * Kp;
+    const PiT* rb = pi + (int64_t)b * Kp;
     const bool y = hy[ed] != 0;
     float s = 0.f, fs = 0.f;
 #pragma unroll
@@ -1178,9 +1211,11 @@ __global__ void __launch_bounds__(256) k_perplexity(Model m, const PiT* __restri
         TR::unpack(ldg_nc_v4(rb + vi * EV), xb);
 #pragma unroll
         for (int e = 0; e < EV; ++e) {
-          const float f = xa[e] * xb[e];
-          fs += f;
-          s += f * (y ? bt[v * EV + e] : (vi * EV + e < K ? 1.0f - bt[v * EV + e] : 0.f));
+          if (vi * EV + e < K) {
+            const float f = xa[e] * xb[e];
+            fs += f;
+            s += f * (y ? bt[v * EV + e] : 1.0f - bt[v * EV + e]);
+          }
         }
       }
     }

@@ -8,14 +8,18 @@
 // prefixes, unrecognised arguments left over as in allow_unregistered), the
 // graph comes from a relativity/SNAP text file (-f, -c relativity), the
 // held-out and test sets are drawn (held-out ratio 0 means 0.1, as
-// learner.cc:87-92), then init() and run() print the reference's perplexity
-// lines.  IO and option errors exit with status 33 (main.cc:79-86).
+// learner.cc:87-92) -- or a network saved before is read back with
+// -c preprocessed -f DIR (network.cc:49-65) --, then init() and run() print
+// the reference's perplexity lines and its PrintStats tables.  IO and
+// option errors exit with status 33 (main.cc:79-86).
 //
 // GB300 additions: -c synthetic takes -f as comma-separated generator
 // parameters (n=5000,k_true=50,size_min=10,size_max=500,intra_degree=4,
 // seed=0, ...); --gb300.pi-dtype f32|bf16, --gb300.chain, --gb300.device,
-// --gb300.graph 0|1, --gb300.verbose; --gb300.save PATH writes a checkpoint
-// of the final chain and --gb300.resume PATH continues a saved one.
+// --gb300.graph 0|1, --gb300.pipeline 0|1, --gb300.verbose; --gb300.save PATH writes a checkpoint
+// of the final chain and --gb300.resume PATH continues a saved one;
+// --gb300.save-network DIR saves the loaded network as the reference's
+// preprocessing tool does (test/preprocess/main.cc, --save).
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -137,9 +141,14 @@ const Spec kSpecs[] = {
     {"gb300.chain", 0, kInt, "chain index (Philox key word)"},
     {"gb300.device", 0, kInt, "CUDA device"},
     {"gb300.graph", 0, kInt, "launch iterations as CUDA graphs (0/1)"},
+    {"gb300.pipeline", 0, kInt,
+     "draw the next iterations on a second stream during the update (1) or in loop order (0)"},
     {"gb300.verbose", 0, kInt, "verbosity"},
     {"gb300.save", 0, kStr, "write a checkpoint of the final state to this file"},
     {"gb300.resume", 0, kStr, "continue the chain saved in this checkpoint"},
+    {"gb300.save-network", 0, kStr,
+     "save the network (graph, held-out and test sets) into this directory; "
+     "read it back with -c preprocessed -f DIR"},
 };
 
 const Spec* find_long(const std::string& name) {
@@ -156,6 +165,7 @@ const Spec* find_short(char c) {
 struct Cli {
   ammsb_options o;
   std::string input_file, input_class = "relativity", config_file, save_path, resume_path;
+  std::string save_network;
   bool contiguous = false, compressed = false;
   std::vector<std::string> remains;
   std::map<std::string, bool> seen;
@@ -200,9 +210,11 @@ struct Cli {
     } else if (n == "gb300.chain") o.chain = (int32_t)parse_int(v, 32, true);
     else if (n == "gb300.device") o.device = (int32_t)parse_int(v, 32, true);
     else if (n == "gb300.graph") o.use_graph = (int32_t)parse_int(v, 32, true);
+    else if (n == "gb300.pipeline") o.pipeline = (int32_t)parse_int(v, 32, true);
     else if (n == "gb300.verbose") o.verbose = (int32_t)parse_int(v, 32, true);
     else if (n == "gb300.save") save_path = v;
     else if (n == "gb300.resume") resume_path = v;
+    else if (n == "gb300.save-network") save_network = v;
   }
 
   void take(const Spec& s, const std::string& v, bool from_config) {
@@ -351,7 +363,8 @@ ammsb_graph_buf* load_graph(const Cli& c) {
     if (ammsb_generate_graph(&p, &g) != AMMSB_OK) throw IOError("graph generation failed");
     return g;
   }
-  throw IOError("unsupported input class '" + c.input_class + "' (relativity or synthetic)");
+  throw IOError("unsupported input class '" + c.input_class +
+                "' (relativity, synthetic or preprocessed)");
 }
 
 }  // namespace
@@ -374,19 +387,36 @@ int main(int argc, char* argv[]) {
   try {
     cli.parse(args);
     for (const auto& r : cli.remains) std::cerr << "ignored argument: " << r << std::endl;
-    g = load_graph(cli);
     double ratio = cli.o.held_out_ratio;
     if (ratio == 0.0) {
       ratio = 0.1;
       std::cerr << "Set held_out_ratio to default " << ratio << std::endl;
     }
+    if (cli.input_class == "preprocessed") {  // network.cc:49-65
+      if (cli.input_file.empty()) throw IOError("no input directory (-f)");
+      double saved_ratio = 0.0;
+      if (ammsb_load_preprocessed(cli.input_file.c_str(), &g, &split, &saved_ratio) != AMMSB_OK)
+        throw IOError("cannot read the preprocessed network in " + cli.input_file);
+      ammsb_graph gv;
+      ammsb_edge_set hv, tv;
+      ammsb_graph_view(g, &gv);
+      ammsb_split_view(split, &hv, &tv);
+      const int64_t want = (int64_t)(ratio * (double)(gv.row_ptr[gv.n] / 2));
+      if (hv.count != 2 * (want / 2))
+        std::cerr << "WARNING: Expect held-out size " << want << ", get " << hv.count << std::endl;
+    } else {
+      g = load_graph(cli);
+      if (ammsb_make_held_out(g, ratio, (uint32_t)cli.o.random_seed, &split) != AMMSB_OK)
+        throw IOError("held-out construction failed");
+    }
     cli.o.held_out_ratio = ratio;
-    if (ammsb_make_held_out(g, ratio, (uint32_t)cli.o.random_seed, &split) != AMMSB_OK)
-      throw IOError("held-out construction failed");
     ammsb_graph graph;
     ammsb_edge_set held, test;
     ammsb_graph_view(g, &graph);
     ammsb_split_view(split, &held, &test);
+    if (!cli.save_network.empty() &&  // the reference's preprocessing tool, --save
+        ammsb_save_preprocessed(&graph, &held, &test, ratio, cli.save_network.c_str()) != AMMSB_OK)
+      throw IOError("cannot save the network into " + cli.save_network);
     std::cout << "start MCMC stochastical" << std::endl;
     if (ammsb_create(&cli.o, &graph, &held, &test, &h) != AMMSB_OK) {
       std::cerr << "MCMC error: " << ammsb_create_error() << std::endl;

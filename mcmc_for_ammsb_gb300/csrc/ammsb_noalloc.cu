@@ -7,23 +7,27 @@
 // allocations, a real-time loop that must not allocate after start-up).
 // They hold pi, beta and the held-out arrays in memory they obtained their
 // own way and need the perplexity of that state.  ammsb_perplexity_noalloc
-// computes it with the same kernel as ammsb_perplexity, keeping the
-// kernel's scratch (per-block compensated partial sums and the result) in
-// a fixed file-scope __device__ array instead of handle-owned memory.
+// computes it with the same kernels as ammsb_perplexity, keeping the
+// kernels' scratch (per-block compensated partial sums, the result and an
+// index-error flag) in a fixed file-scope __device__ array instead of
+// handle-owned memory.
 //
 // The array has room for kMaxBlocks partials and the kernel runs one block
 // per 256 held-out edges, so one call accepts at most kMaxBlocks * 256 =
 // 4,194,304 held-out edges and rejects more with AMMSB_E_CAPACITY (the
-// message goes to stderr, as do those of the other rejected arguments).  The array lives in
-// every GPU that loads the library, until the process exits.  All calls on
-// a device share it and it keeps the last call's contents: every call
-// writes the partials it reads, so nothing has to be cleared, but calls
-// whose kernels overlap on the GPU race on it.  The first call on a device
-// looks up the array's device address (cudaGetSymbolAddress) with that
-// device current; make that first call before any stream capture.
+// message goes to stderr, as do those of the other rejected arguments).
+// The array lives in every GPU that loads the library, until the process
+// exits.  All calls on a device share it and it keeps the last call's
+// contents: every call writes the partials it reads and clears the flag
+// before its kernels run, but calls whose kernels overlap on the GPU race
+// on it.  The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress) with that device current.  Every call ends by
+// copying the result into pageable host memory and synchronising its
+// stream, so it cannot be called on a stream that is being captured.
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -38,8 +42,11 @@ constexpr int kMaxBlocks = 16384;
 constexpr int kEdgesPerBlock = 256;
 constexpr int kMaxDevices = 64;
 
-// partial (sum, compensation) per block, then the result (2 doubles)
-static __device__ __align__(256) double g_ppx_scratch[2 * kMaxBlocks + 2];
+// partial (sum, compensation) per block, then the result (2 doubles), then
+// the index-error flag (one double's room)
+static __device__ __align__(256) double g_ppx_scratch[2 * kMaxBlocks + 3];
+constexpr int kResult = 2 * kMaxBlocks;
+constexpr int kFlag = 2 * kMaxBlocks + 2;
 
 std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
@@ -53,21 +60,23 @@ int next_pow2i(int v) {
 template <typename PiT, int LPN, int VPL>
 cudaError_t launch(const Model& m, const void* pi, const float* beta, const int32_t* ha,
                    const int32_t* hb, const uint8_t* hy, int64_t H, float* ppx, float count,
-                   double* scratch, int nblk, cudaStream_t s) {
-  k_perplexity<PiT, LPN, VPL><<<nblk, 256, 0, s>>>(m, reinterpret_cast<const PiT*>(pi), beta, ha,
-                                                   hb, hy, H, ppx, count, scratch);
+                   double* scratch, int nblk, int64_t n_rows, cudaStream_t s) {
+  k_perplexity<PiT, LPN, VPL><<<nblk, 256, 0, s>>>(
+      m, reinterpret_cast<const PiT*>(pi), beta, ha, hb, hy, H, ppx, count, scratch, n_rows,
+      reinterpret_cast<unsigned int*>(scratch + kFlag));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_ppx_final<<<1, kPpxFinalThreads, 0, s>>>(scratch, nblk, H, scratch + 2 * kMaxBlocks);
+  k_ppx_final<<<1, kPpxFinalThreads, 0, s>>>(scratch, nblk, H, scratch + kResult);
   return cudaGetLastError();
 }
 
 template <typename PiT>
 cudaError_t dispatch(int lpn, int vpl, const Model& m, const void* pi, const float* beta,
                      const int32_t* ha, const int32_t* hb, const uint8_t* hy, int64_t H, float* ppx,
-                     float count, double* scratch, int nblk, cudaStream_t s) {
+                     float count, double* scratch, int nblk, int64_t n_rows, cudaStream_t s) {
 #define CASE(L, V) \
-  if (lpn == L && vpl == V) return launch<PiT, L, V>(m, pi, beta, ha, hb, hy, H, ppx, count, scratch, nblk, s);
+  if (lpn == L && vpl == V)  \
+    return launch<PiT, L, V>(m, pi, beta, ha, hb, hy, H, ppx, count, scratch, nblk, n_rows, s);
   CASE(1, 1) CASE(2, 1) CASE(4, 1) CASE(8, 1) CASE(16, 1) CASE(32, 1) CASE(32, 2) CASE(32, 4) CASE(32, 8)
 #undef CASE
   return cudaErrorInvalidConfiguration;
@@ -78,7 +87,7 @@ cudaError_t dispatch(int lpn, int vpl, const Model& m, const void* pi, const flo
 extern "C" {
 
 int ammsb_perplexity_noalloc(const void* pi, int32_t pi_dtype, int64_t K, int64_t row_stride,
-                             const float* beta, double epsilon, const int32_t* held_a,
+                             int64_t n_rows, const float* beta, double epsilon, const int32_t* held_a,
                              const int32_t* held_b, const uint8_t* held_y, int64_t held_count,
                              float* ppx, uint64_t average_count, void* stream, double* out) {
   auto fail = [](const std::string& msg, int code) {
@@ -96,6 +105,8 @@ int ammsb_perplexity_noalloc(const void* pi, int32_t pi_dtype, int64_t K, int64_
                 AMMSB_E_ARG);
   if ((reinterpret_cast<uintptr_t>(pi) & 15) != 0)
     return fail("pi must be 16-byte aligned", AMMSB_E_ARG);
+  if (n_rows < 1 || n_rows > (int64_t)INT32_MAX + 1)
+    return fail("n_rows must be in [1, 2^31]", AMMSB_E_ARG);
   if (held_count < 0 || held_count > (int64_t)kMaxBlocks * kEdgesPerBlock)
     return fail("held_count exceeds the static scratch: at most 4,194,304 held-out edges",
                 AMMSB_E_CAPACITY);
@@ -122,9 +133,9 @@ int ammsb_perplexity_noalloc(const void* pi, int32_t pi_dtype, int64_t K, int64_
   }
   Model m{};
   m.K = (int32_t)K;
-  m.Kp = (int32_t)row_stride;
+  m.Kp = (int32_t)row_stride;  // addressing only: the kernel reads the K values of a row
   m.epsilon = (float)epsilon;
-  const int nvec = (int)(row_stride / ev);
+  const int nvec = (int)((K + ev - 1) / ev);
   int lpn, vpl;
   if (nvec <= 32) {
     lpn = next_pow2i(nvec);
@@ -133,18 +144,27 @@ int ammsb_perplexity_noalloc(const void* pi, int32_t pi_dtype, int64_t K, int64_
     lpn = 32;
     vpl = next_pow2i((nvec + 31) / 32);
   }
-  if (vpl > 8) return fail("row too wide", AMMSB_E_ARG);
+  if (vpl > 8) return fail("row too wide", AMMSB_E_ARG);  // K <= 1024 keeps vpl <= 8
   const int nblk = (int)((held_count + kEdgesPerBlock - 1) / kEdgesPerBlock);
   const float count = (float)average_count;
-  cudaError_t e = (pi_dtype == AMMSB_PI_BF16)
-                      ? dispatch<__nv_bfloat16>(lpn, vpl, m, pi, beta, held_a, held_b, held_y,
-                                                held_count, ppx, count, scratch, nblk, s)
-                      : dispatch<float>(lpn, vpl, m, pi, beta, held_a, held_b, held_y, held_count,
-                                        ppx, count, scratch, nblk, s);
+  cudaError_t e = cudaMemsetAsync(scratch + kFlag, 0, sizeof(double), s);
+  if (e != cudaSuccess) return fail(std::string("flag clear: ") + cudaGetErrorString(e), AMMSB_E_CUDA);
+  e = (pi_dtype == AMMSB_PI_BF16)
+          ? dispatch<__nv_bfloat16>(lpn, vpl, m, pi, beta, held_a, held_b, held_y, held_count, ppx,
+                                    count, scratch, nblk, n_rows, s)
+          : dispatch<float>(lpn, vpl, m, pi, beta, held_a, held_b, held_y, held_count, ppx, count,
+                            scratch, nblk, n_rows, s);
   if (e != cudaSuccess) return fail(std::string("launch: ") + cudaGetErrorString(e), AMMSB_E_CUDA);
-  e = cudaMemcpyAsync(out, scratch + 2 * kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s);
+  double res[3];  // result (2 doubles: value, compensation) and the flag
+  e = cudaMemcpyAsync(res, scratch + kResult, sizeof(res), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(std::string("result copy: ") + cudaGetErrorString(e), AMMSB_E_CUDA);
+  unsigned int flag = 0;
+  std::memcpy(&flag, &res[2], sizeof(flag));
+  if (flag != 0)
+    return fail("a held-out pair names a row outside [0, n_rows): those pairs were skipped",
+                AMMSB_E_ARG);
+  *out = res[0];
   return AMMSB_OK;
 }
 

@@ -15,6 +15,10 @@
 #pragma once
 #include "ammsb_kernels.cuh"
 
+#ifndef AMMSB_RING_WARP_PROLOGUE
+#define AMMSB_RING_WARP_PROLOGUE 0
+#endif
+
 namespace ammsb {
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -216,86 +220,150 @@ __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffe
       if (t < T) copy_row_lane<PiT, VPL, FULL>(my_ring + (size_t)t * Kp, pi + (int64_t)j0[t] * Kp, lane, nvec);
       cp_async_commit();
     }
-    // ---- node prologue: S = sum phi, s_i = sum pi, w = pi * (beta - eps)
-    float S = 0.f;
-    if constexpr (STASH) {
-      for (int q = tid; q < n_out; q += NT) s_nb[q] = nbr_g[q];
+    float S, si;
+    f32x2 w2[NP], A2[NP];
+    if constexpr (STASH && AMMSB_RING_WARP_PROLOGUE) {
+      // ---- node prologue, per warp (BF16 rows): every warp reads the whole
+      // phi row in its lanes' vector layout and forms S = sum phi,
+      // s_i = sum pi and w = pi * (beta - eps) with shuffles alone -- the same
+      // operations on the same values in every warp, so the warps agree bit
+      // for bit without a CTA barrier; the thread's own epilogue elements
+      // (phi and the normals) go to its private stash places
+      // the neighbour words of this warp's rows (q = warp + SPLIT t), which
+      // only this warp reads
+      for (int t = lane; t < T; t += 32) s_nb[warp + SPLIT * t] = nbr_g[warp + SPLIT * t];
 #pragma unroll
       for (int g = 0; g < NG; ++g) {
         const int k0 = 4 * (tid + NT * g);
         if (k0 < K) *reinterpret_cast<float4*>(s_nz + k0) = phi_normals(b, rs, slot, i, step, k0, K);
+        if (k0 < Kp) *reinterpret_cast<float4*>(s_phi + k0) = ph[g];
       }
+      float phv[EPL];
 #pragma unroll
-      for (int g = 0; g < NG; ++g) S += (ph[g].x + ph[g].y) + (ph[g].z + ph[g].w);
-    } else {
-      for (int k = tid; k < Kp; k += NT) S += phi_i[k];
-      for (int q = tid; q < n_out; q += NT) s_nb[q] = nbr_g[q];
-    }
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = lane + 32 * v;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
-    if (lane == 0) s_red[warp] = S;
-    __syncthreads();
-    S = 0.f;
-#pragma unroll
-    for (int w = 0; w < SPLIT; ++w) S += s_red[w];
-    float si = 0.f;
-    if constexpr (STASH) {
-      const float rS = 1.0f / S;  // pi = phi / S as phi * (1/S): within 1 ulp
-#pragma unroll
-      for (int g = 0; g < NG; ++g) {
-        const int k0 = 4 * (tid + NT * g);
-        if (k0 < Kp) {
-          const float4 bt = *reinterpret_cast<const float4*>(b.beta + k0);
-          float4 p, wv;
-          p.x = ph[g].x * rS;
-          p.y = ph[g].y * rS;
-          p.z = ph[g].z * rS;
-          p.w = ph[g].w * rS;
-          si += p.x;
-          si += p.y;
-          si += p.z;
-          si += p.w;
-          wv.x = (k0 + 0 < K) ? p.x * (bt.x - m.epsilon) : 0.f;
-          wv.y = (k0 + 1 < K) ? p.y * (bt.y - m.epsilon) : 0.f;
-          wv.z = (k0 + 2 < K) ? p.z * (bt.z - m.epsilon) : 0.f;
-          wv.w = (k0 + 3 < K) ? p.w * (bt.w - m.epsilon) : 0.f;
-          *reinterpret_cast<float4*>(s_w + k0) = wv;
-          *reinterpret_cast<float4*>(s_phi + k0) = ph[g];
+        for (int e = 0; e < EV; e += 4) {
+          const float4 q = (FULL || vi < nvec) ? *reinterpret_cast<const float4*>(phi_i + vi * EV + e)
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+          phv[v * EV + e] = q.x;
+          phv[v * EV + e + 1] = q.y;
+          phv[v * EV + e + 2] = q.z;
+          phv[v * EV + e + 3] = q.w;
         }
       }
+      S = 0.f;
+#pragma unroll
+      for (int e = 0; e < EPL; e += 4) S += (phv[e] + phv[e + 1]) + (phv[e + 2] + phv[e + 3]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+      const float rS = 1.0f / S;  // pi = phi / S as phi * (1/S): within 1 ulp
+      si = 0.f;
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = lane + 32 * v;
+#pragma unroll
+        for (int e = 0; e < EV; e += 4) {
+          float4 bt = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (FULL || vi < nvec) bt = *reinterpret_cast<const float4*>(b.beta + vi * EV + e);
+          const int kb = vi * EV + e;
+          float pv[4], wv[4];
+          const float btv[4] = {bt.x, bt.y, bt.z, bt.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            pv[u] = phv[v * EV + e + u] * rS;
+            si += pv[u];
+            wv[u] = (kb + u < K) ? pv[u] * (btv[u] - m.epsilon) : 0.f;
+          }
+          w2[(v * EV + e) / 2] = pack_f32x2(wv[0], wv[1]);
+          w2[(v * EV + e) / 2 + 1] = pack_f32x2(wv[2], wv[3]);
+          A2[(v * EV + e) / 2] = 0ull;
+          A2[(v * EV + e) / 2 + 1] = 0ull;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) si += __shfl_xor_sync(0xffffffffu, si, o);
+      __syncwarp();  // the warp's neighbour words are in
     } else {
-      for (int k = tid; k < Kp; k += NT) {
-        const float p = __fdiv_rn(phi_i[k], S);
-        si += p;
-        s_w[k] = (k < K) ? p * (b.beta[k] - m.epsilon) : 0.f;
+      // ---- node prologue: S = sum phi, s_i = sum pi, w = pi * (beta - eps)
+      S = 0.f;
+      if constexpr (STASH) {
+        for (int q = tid; q < n_out; q += NT) s_nb[q] = nbr_g[q];
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          const int k0 = 4 * (tid + NT * g);
+          if (k0 < K) *reinterpret_cast<float4*>(s_nz + k0) = phi_normals(b, rs, slot, i, step, k0, K);
+        }
+#pragma unroll
+        for (int g = 0; g < NG; ++g) S += (ph[g].x + ph[g].y) + (ph[g].z + ph[g].w);
+      } else {
+        for (int k = tid; k < Kp; k += NT) S += phi_i[k];
+        for (int q = tid; q < n_out; q += NT) s_nb[q] = nbr_g[q];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+      if (lane == 0) s_red[warp] = S;
+      __syncthreads();
+      S = 0.f;
+#pragma unroll
+      for (int w = 0; w < SPLIT; ++w) S += s_red[w];
+      si = 0.f;
+      if constexpr (STASH) {
+        const float rS = 1.0f / S;  // pi = phi / S as phi * (1/S): within 1 ulp
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          const int k0 = 4 * (tid + NT * g);
+          if (k0 < Kp) {
+            const float4 bt = *reinterpret_cast<const float4*>(b.beta + k0);
+            float4 p, wv;
+            p.x = ph[g].x * rS;
+            p.y = ph[g].y * rS;
+            p.z = ph[g].z * rS;
+            p.w = ph[g].w * rS;
+            si += p.x;
+            si += p.y;
+            si += p.z;
+            si += p.w;
+            wv.x = (k0 + 0 < K) ? p.x * (bt.x - m.epsilon) : 0.f;
+            wv.y = (k0 + 1 < K) ? p.y * (bt.y - m.epsilon) : 0.f;
+            wv.z = (k0 + 2 < K) ? p.z * (bt.z - m.epsilon) : 0.f;
+            wv.w = (k0 + 3 < K) ? p.w * (bt.w - m.epsilon) : 0.f;
+            *reinterpret_cast<float4*>(s_w + k0) = wv;
+            *reinterpret_cast<float4*>(s_phi + k0) = ph[g];
+          }
+        }
+      } else {
+        for (int k = tid; k < Kp; k += NT) {
+          const float p = __fdiv_rn(phi_i[k], S);
+          si += p;
+          s_w[k] = (k < K) ? p * (b.beta[k] - m.epsilon) : 0.f;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) si += __shfl_xor_sync(0xffffffffu, si, o);
+      if (lane == 0) s_red[SPLIT + warp] = si;
+      __syncthreads();
+      si = 0.f;
+#pragma unroll
+      for (int w = 0; w < SPLIT; ++w) si += s_red[SPLIT + w];
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        const int vi = lane + 32 * v;
+#pragma unroll
+        for (int e = 0; e < EV; e += 4) {
+          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (FULL || vi < nvec) q = *reinterpret_cast<const float4*>(s_w + vi * EV + e);
+          w2[(v * EV + e) / 2] = pack_f32x2(q.x, q.y);
+          w2[(v * EV + e) / 2 + 1] = pack_f32x2(q.z, q.w);
+          A2[(v * EV + e) / 2] = 0ull;
+          A2[(v * EV + e) / 2 + 1] = 0ull;
+        }
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) si += __shfl_xor_sync(0xffffffffu, si, o);
-    if (lane == 0) s_red[SPLIT + warp] = si;
-    __syncthreads();
-    si = 0.f;
-#pragma unroll
-    for (int w = 0; w < SPLIT; ++w) si += s_red[SPLIT + w];
     // the per-row constants of y = 1 and y = 0
     const float one_m_si = 1.0f - si;
     const float e1si = m.epsilon * si, e0si = (1.0f - m.epsilon) * si;
     const float e1o = m.epsilon * one_m_si, e0o = (1.0f - m.epsilon) * one_m_si;
-
-    f32x2 w2[NP], A2[NP];
-#pragma unroll
-    for (int v = 0; v < VPL; ++v) {
-      const int vi = lane + 32 * v;
-#pragma unroll
-      for (int e = 0; e < EV; e += 4) {
-        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (FULL || vi < nvec) q = *reinterpret_cast<const float4*>(s_w + vi * EV + e);
-        w2[(v * EV + e) / 2] = pack_f32x2(q.x, q.y);
-        w2[(v * EV + e) / 2 + 1] = pack_f32x2(q.z, q.w);
-        A2[(v * EV + e) / 2] = 0ull;
-        A2[(v * EV + e) / 2 + 1] = 0ull;
-      }
-    }
     // neighbour word of the row in each ring slot
     uint32_t nbw[STAGES];
 #pragma unroll
@@ -456,15 +524,18 @@ __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffe
 // Iterations with few nodes (the link stratum: one vertex and its edges)
 // take a 16-warp variant, whose warps each hold a quarter of the rows the
 // 4-warp one gives them, so a node's rows are in flight together.
+// Blocks per SM the register budget is sized for: 16 warps per SM.
+template <int SPLIT>
+constexpr int ring_min_blocks() { return SPLIT >= 16 ? 1 : 16 / SPLIT; }
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
-__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1)
+__global__ void __launch_bounds__(SPLIT * 32, ring_min_blocks<SPLIT>())
     k_update_phi_ring(Model m, Buffers b, int n_lo, int n_hi) {
   const int n_nodes = b.st->n_nodes;
   if (n_nodes <= n_lo || n_nodes > n_hi) return;
   update_phi_ring_body<PiT, VPL, SPLIT, STAGES, FULL>(m, b);
 }
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
-__global__ void __launch_bounds__(SPLIT * 32, (SPLIT * 32 * 128 <= 16384) ? 4 : 1)
+__global__ void __launch_bounds__(SPLIT * 32, ring_min_blocks<SPLIT>())
     k_update_phi_ring_chains(const ChainArgs* __restrict__ c, int p, int n_lo, int n_hi) {
   const ChainArgs& a = c[blockIdx.y];
   const int n_nodes = a.b[p].st->n_nodes;

@@ -79,6 +79,44 @@ class Network:
                                               ctypes.byref(buf)))
         return Network._from_buf(buf)
 
+    @staticmethod
+    def load_preprocessed(dirname):
+        """A network saved by save_preprocessed (the reference's input class
+        "preprocessed", network.cc:49-65): graph, held-out and test sets;
+        the held-out ratio it was drawn with is `held_out_ratio`."""
+        L = _native.lib()
+        g = ctypes.c_void_p()
+        sp = ctypes.c_void_p()
+        ratio = ctypes.c_double()
+        _native.check(L.ammsb_load_preprocessed(str(dirname).encode(), ctypes.byref(g),
+                                                ctypes.byref(sp), ctypes.byref(ratio)))
+        net = Network._from_buf(g)
+        try:
+            h = _native.AmmsbEdgeSet()
+            t = _native.AmmsbEdgeSet()
+            L.ammsb_split_view(sp, ctypes.byref(h), ctypes.byref(t))
+            net.held_out = (_as_np(h.a, h.count, np.int32), _as_np(h.b, h.count, np.int32),
+                            _as_np(h.y, h.count, np.uint8))
+            net.test = (_as_np(t.a, t.count, np.int32), _as_np(t.b, t.count, np.int32),
+                        _as_np(t.y, t.count, np.uint8))
+        finally:
+            L.ammsb_split_free(sp)
+        net.held_out_ratio = ratio.value
+        return net
+
+    def save_preprocessed(self, dirname, held_out_ratio=None):
+        """Network::save (network.cc:136-145): the graph, the held-out and
+        test sets and the auxiliary data into directory `dirname` (see
+        ammsb_save_preprocessed)."""
+        ratio = held_out_ratio if held_out_ratio is not None else getattr(self, "held_out_ratio",
+                                                                          0.0)
+        ho, _keep_h = Network.native_edge_set(self.held_out)
+        te, _keep_t = Network.native_edge_set(self.test)
+        g = self.native_graph()
+        _native.check(_native.lib().ammsb_save_preprocessed(
+            ctypes.byref(g), ctypes.byref(ho), ctypes.byref(te), float(ratio),
+            str(dirname).encode()))
+
     def _with_buf(self, fn):
         """Run fn(graph_buf) on the native graph (built from the CSR if this
         Network was not made by the native library)."""
@@ -104,6 +142,7 @@ class Network:
     def make_held_out(self, held_out_ratio, seed=0):
         """network.cc:503-614 (see ammsb_make_held_out); sets held_out, test."""
         L = _native.lib()
+        self.held_out_ratio = held_out_ratio
 
         def run(buf):
             sp = ctypes.c_void_p()

@@ -102,6 +102,7 @@ _SPEC = [
     ("gb300.chain", None, "chain", "int", 0),
     ("gb300.device", None, "device", "int", 0),
     ("gb300.graph", None, "use_graph", "int", 1),
+    ("gb300.pipeline", None, "pipeline", "int", 1),
     ("gb300.verbose", None, "verbose", "int", 0),
 ]
 _BY_LONG = {s[0]: s for s in _SPEC}

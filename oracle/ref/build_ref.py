@@ -4,8 +4,8 @@ oracle/ref/shim and the harness oracle/ref/ref_harness.cc into
 oracle/_ref/libammsb_ref.so.
 
 TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie
-(AMMSB_REFERENCE_ROOT, default /root/reference) and writes only into
-oracle/_ref/.  Missing third-party headers (Boost program_options,
+(AMMSB_REFERENCE_ROOT, else a `reference` checkout beside this repository's
+directory) and writes only into oracle/_ref/.  Missing third-party headers (Boost program_options,
 circular_buffer, filesystem, iostreams; google sparsehash; tinyxml2) are
 replaced by the small shims; OpenMP and MPI are off (the reference's SEQ
 build); Float = float (MCMC_SINGLE_PRECISION, the reference default); the
@@ -20,7 +20,9 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 LIB = os.path.join(OUT, "libammsb_ref.so")
-REFERENCE_ROOT = os.environ.get("AMMSB_REFERENCE_ROOT", "/root/reference")
+REPO = os.path.dirname(os.path.dirname(HERE))
+REFERENCE_ROOT = os.environ.get("AMMSB_REFERENCE_ROOT",
+                                os.path.join(os.path.dirname(REPO), "reference"))
 SRC_ROOT = os.path.join(REFERENCE_ROOT, "c++", "src")
 SOURCES = ["np", "options", "exception", "random", "data", "network", "timer",
            "preprocess/dataset", "preprocess/relativity", "preprocess/data_factory",

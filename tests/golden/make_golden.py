@@ -1,7 +1,7 @@
 """Generates tests/golden/ref_*.npz from the reference's own sampler code.
 
-Builds oracle/_ref/libammsb_ref.so from the reference sources (needs them
-under /root/reference; see oracle/ref/build_ref.py) and records, for small
+Builds oracle/_ref/libammsb_ref.so from the reference sources (where
+oracle/ref/build_ref.py finds them) and records, for small
 fixed workloads, what the reference's functions return:
 
   * the graph, held-out and test sets as the reference loaded/drew them;
