@@ -146,6 +146,40 @@ int ammsb_step_fed(ammsb_handle *h, uint32_t step, int32_t n_edges,
                    const uint8_t *nbr_y, const float *phi_noise,
                    const float *theta_noise);
 
+/* One rank's phases of a sharded iteration.  They replace the distributed
+ * sampler's per-iteration split (mcmc_sampler_stochastic_distr.cc:630-708:
+ * minibatch nodes owned by node % ranks, distr.cc:1626-1632; the updated pi
+ * rows written to the shared store; the beta gradient summed over ranks,
+ * distr.cc:1430-1442): every rank holds all of pi, updates the phi rows of
+ * the nodes it owns, and the caller moves rows and sums between ranks.
+ *   ammsb_shard_draw    the minibatch and neighbour sets of iteration
+ *                       step_count, the same on every rank (they depend only
+ *                       on seed, chain and step); ammsb_get_last_minibatch
+ *                       reads them;
+ *   ammsb_shard_update  update_phi of the owned slots (ascending indices into
+ *                       the drawn nodes); writes their new pi rows (FP32,
+ *                       n_owned x K) to rows_out;
+ *   ammsb_shard_commit  every drawn node's new pi row (FP32, n_nodes x K in
+ *                       slot order, gathered from all ranks) committed into
+ *                       pi, then the beta-gradient sums R (K x 2: sum of
+ *                       f_k / P over the y = 0 and the y = 1 edges) over the
+ *                       owned edges (ascending indices into the drawn edges)
+ *                       written to R_out;
+ *   ammsb_shard_theta   the theta step (update_beta, cc:241-266) from the sums
+ *                       added over all ranks; the iteration is done and
+ *                       step_count advances.
+ * The calls must come in this order; each synchronises the handle's stream.
+ * Host arrays throughout.  A single rank that owns every node and edge
+ * takes the same iteration as ammsb_step, up to the order in which the
+ * beta sums are added. */
+int ammsb_shard_draw(ammsb_handle *h);
+int ammsb_shard_update(ammsb_handle *h, int32_t n_owned, const int32_t *slots,
+                       float *rows_out);
+int ammsb_shard_commit(ammsb_handle *h, const float *rows_all,
+                       int32_t n_owned_edges, const int32_t *edge_idx,
+                       double *R_out);
+int ammsb_shard_theta(ammsb_handle *h, const double *R_total);
+
 /* Learner::cal_perplexity_held_out (learner.cc:128, 138-183): running
  * average per held-out edge, -mean log; advances average_count. */
 int ammsb_perplexity(ammsb_handle *h, double *out);

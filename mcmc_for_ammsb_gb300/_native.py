@@ -169,6 +169,10 @@ SIGNATURES = [
                                            ctypes.POINTER(_P)]),
     ("ammsb_split_view", None, [_P, ctypes.POINTER(AmmsbEdgeSet), ctypes.POINTER(AmmsbEdgeSet)]),
     ("ammsb_split_free", None, [_P]),
+    ("ammsb_shard_draw", ctypes.c_int, [_P]),
+    ("ammsb_shard_update", ctypes.c_int, [_P, ctypes.c_int32, _I32P, _F32P]),
+    ("ammsb_shard_commit", ctypes.c_int, [_P, _F32P, ctypes.c_int32, _I32P, _F64P]),
+    ("ammsb_shard_theta", ctypes.c_int, [_P, _F64P]),
     ("ammsb_save_preprocessed", ctypes.c_int, [ctypes.POINTER(AmmsbGraph),
                                                ctypes.POINTER(AmmsbEdgeSet),
                                                ctypes.POINTER(AmmsbEdgeSet), ctypes.c_double,

@@ -104,19 +104,11 @@ cudaError_t launch_phi_ring_t(ammsb_handle* h, const Buffers& b, bool configure)
     return cudaSuccess;
   }
   if (use_wide) {
-    // the node count on the device picks the variant that works; the other
-    // returns at once.  They run as parallel branches (a fork onto phi_aux
-    // and a join), so the empty launch does not lengthen the iteration.
-    cudaError_t e = cudaEventRecord(h->ev_phi_fork, h->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->phi_aux, h->ev_phi_fork, 0);
-    if (e != cudaSuccess) return e;
-    wide<<<std::min(kRingFewNodes, h->m.max_nodes), kRingSplitWide * 32, smem_w, h->phi_aux>>>(
+    wide<<<std::min(kRingFewNodes, h->m.max_nodes), kRingSplitWide * 32, smem_w, h->stream>>>(
         h->m, b, 0, kRingFewNodes);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, kRingFewNodes, INT32_MAX);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(h->ev_phi_join, h->phi_aux)) != cudaSuccess) return e;
-    return cudaStreamWaitEvent(h->stream, h->ev_phi_join, 0);
   } else {
     kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, 0, INT32_MAX);
   }
@@ -492,7 +484,6 @@ void ammsb_destroy(ammsb_handle* h) {
       if (set[s]) cudaGraphExecDestroy(set[s]);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->side) cudaStreamSynchronize(h->side);
-  if (h->phi_aux) cudaStreamSynchronize(h->phi_aux);
   for (auto& per_n : h->ev_phase)
     for (auto& set : per_n)
       for (auto& e : set)
@@ -500,9 +491,6 @@ void ammsb_destroy(ammsb_handle* h) {
   for (void* p : h->allocs) cudaFree(p);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
-  if (h->ev_phi_fork) cudaEventDestroy(h->ev_phi_fork);
-  if (h->ev_phi_join) cudaEventDestroy(h->ev_phi_join);
-  if (h->phi_aux) cudaStreamDestroy(h->phi_aux);
   if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -589,11 +577,8 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h->phi_aux, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h->ev_phi_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h->ev_phi_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
     h->err = "cudaStreamCreate / cudaEventCreate failed";
     return bail(AMMSB_E_CUDA);
   }
@@ -1446,6 +1431,187 @@ int ammsb_get_kernel_config(ammsb_handle* h, int32_t* out) {
 }
 
 void* ammsb_stream(ammsb_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+// ---------------------------------------------------------------------------
+// Sharded iteration (the distributed sampler's split of one iteration over
+// ranks, mcmc_sampler_stochastic_distr.cc): every rank draws the same
+// minibatch and neighbour sets (they depend only on seed, chain and step),
+// updates the phi rows of the minibatch nodes it owns, all ranks exchange
+// the new pi rows, each commits all of them into its own pi and sums the
+// beta gradient over the edges it owns, the ranks add those sums, and each
+// takes the same theta step.  These four calls are one rank's phases; the
+// exchange between them is the caller's (mcmc_for_ammsb_gb300/sharded.py).
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+__global__ void k_shard_gather_nodes(Buffers from, Buffers to, const int32_t* slots, int n, int n_out) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < (int64_t)n * n_out;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(x / n_out), j = (int)(x % n_out);
+    const int s = slots[q];
+    to.nbr[x] = from.nbr[(int64_t)s * n_out + j];
+    if (j == 0) to.nodes[q] = from.nodes[s];
+  }
+}
+
+__global__ void k_shard_gather_edges(Buffers from, Buffers to, const int32_t* idx, int n, int n_nodes) {
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+    to.ea[x] = from.ea[idx[x]];
+    to.eb[x] = from.eb[idx[x]];
+    to.ey[x] = from.ey[idx[x]];
+  }
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n_nodes; x += gridDim.x * blockDim.x)
+    to.nodes[x] = from.nodes[x];
+}
+
+int shard_buffers(ammsb_handle* h) {
+  if (!h->d_shard_idx) {
+    const size_t n = (size_t)std::max<int64_t>(h->m.max_nodes, h->m.max_edges);
+    int rc = dev_alloc(h, &h->d_shard_idx, n);
+    if (!rc) rc = dev_alloc(h, &h->d_shard_R, (size_t)2 * h->m.K);
+    if (rc) return rc;
+  }
+  return AMMSB_OK;
+}
+
+DevState read_state(ammsb_handle* h, const Buffers& b, int* rc) {
+  DevState st{};
+  *rc = AMMSB_OK;
+  if (cudaMemcpyAsync(&st, b.st, sizeof(st), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    h->err = "state read failed";
+    *rc = AMMSB_E_CUDA;
+  }
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ammsb_shard_draw(ammsb_handle* h) {
+  if (!h) return AMMSB_E_ARG;
+  if (!h->state_ready) {
+    h->err = "call ammsb_init_state or ammsb_set_state first";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  int rc = shard_buffers(h);
+  if (rc) return rc;
+  h->ahead = 0;  // nothing drawn ahead survives: the draw is for step_count
+  const uint32_t s = (uint32_t)h->step_count;
+  CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+  CK(launch_sampling_phase(h, h->bufs[h->slot], h->stream));
+  h->shard_drawn = h->slot;
+  h->last = h->slot;
+  h->shard_phase = 1;
+  return check_device_err(h);
+}
+
+int ammsb_shard_update(ammsb_handle* h, int32_t n_owned, const int32_t* slots, float* rows_out) {
+  if (!h || n_owned < 0 || (n_owned > 0 && (!slots || !rows_out))) return AMMSB_E_ARG;
+  if (h->shard_phase != 1) {
+    h->err = "ammsb_shard_update follows ammsb_shard_draw";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  const Buffers& D = h->bufs[h->shard_drawn];
+  int rc = AMMSB_OK;
+  DevState st = read_state(h, D, &rc);
+  if (rc) return rc;
+  if (n_owned > st.n_nodes) return AMMSB_E_ARG;
+  for (int32_t q = 0; q < n_owned; ++q)
+    if (slots[q] < 0 || slots[q] >= st.n_nodes || (q > 0 && slots[q] <= slots[q - 1])) {
+      h->err = "owned slots must be ascending and inside the drawn minibatch";
+      return AMMSB_E_ARG;
+    }
+  h->shard_phase = 2;
+  if (n_owned == 0) return AMMSB_OK;
+  // the owned nodes and their neighbour sets, compacted into the next
+  // buffer set, then update_phi of those alone
+  const Buffers& W = h->bufs[(h->shard_drawn + 1) % kRing];
+  CK(cudaMemcpyAsync(h->d_shard_idx, slots, sizeof(int32_t) * n_owned, cudaMemcpyHostToDevice, h->stream));
+  const int64_t work = (int64_t)n_owned * h->m.n_out;
+  k_shard_gather_nodes<<<(int)std::min<int64_t>((work + 255) / 256, 152 * 8), 256, 0, h->stream>>>(
+      D, W, h->d_shard_idx, n_owned, h->m.n_out);
+  CK(cudaGetLastError());
+  DevState ws = st;
+  ws.n_nodes = n_owned;
+  ws.n_edges = 0;
+  CK(cudaMemcpyAsync(W.st, &ws, sizeof(ws), cudaMemcpyHostToDevice, h->stream));
+  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_phi<__nv_bfloat16>(h, W) : launch_phi<float>(h, W));
+  CK(cudaMemcpy2DAsync(rows_out, sizeof(float) * h->m.K, h->b.stage, sizeof(float) * h->m.Kp,
+                       sizeof(float) * h->m.K, n_owned, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return check_device_err(h);
+}
+
+int ammsb_shard_commit(ammsb_handle* h, const float* rows_all, int32_t n_owned_edges,
+                       const int32_t* edge_idx, double* R_out) {
+  if (!h || !rows_all || !R_out || n_owned_edges < 0 || (n_owned_edges > 0 && !edge_idx))
+    return AMMSB_E_ARG;
+  if (h->shard_phase != 2) {
+    h->err = "ammsb_shard_commit follows ammsb_shard_update";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  const Buffers& D = h->bufs[h->shard_drawn];
+  int rc = AMMSB_OK;
+  DevState st = read_state(h, D, &rc);
+  if (rc) return rc;
+  for (int32_t q = 0; q < n_owned_edges; ++q)
+    if (edge_idx[q] < 0 || edge_idx[q] >= st.n_edges || (q > 0 && edge_idx[q] <= edge_idx[q - 1])) {
+      h->err = "owned edges must be ascending and inside the drawn minibatch";
+      return AMMSB_E_ARG;
+    }
+  // every node's new pi row into the staging rows (slot order), the owned
+  // edges into the next buffer set beside all the nodes, then the commit of
+  // every row and the beta partials of the owned edges
+  CK(cudaMemcpy2DAsync(h->b.stage, sizeof(float) * h->m.Kp, rows_all, sizeof(float) * h->m.K,
+                       sizeof(float) * h->m.K, st.n_nodes, cudaMemcpyHostToDevice, h->stream));
+  const Buffers& W = h->bufs[(h->shard_drawn + 1) % kRing];
+  if (n_owned_edges > 0)
+    CK(cudaMemcpyAsync(h->d_shard_idx, edge_idx, sizeof(int32_t) * n_owned_edges, cudaMemcpyHostToDevice,
+                       h->stream));
+  const int span = std::max(n_owned_edges, st.n_nodes);
+  k_shard_gather_edges<<<std::max(1, std::min((span + 255) / 256, 152 * 8)), 256, 0, h->stream>>>(
+      D, W, h->d_shard_idx, n_owned_edges, st.n_nodes);
+  CK(cudaGetLastError());
+  DevState ws = st;
+  ws.n_edges = n_owned_edges;
+  CK(cudaMemcpyAsync(W.st, &ws, sizeof(ws), cudaMemcpyHostToDevice, h->stream));
+  CK(h->opt.pi_dtype == AMMSB_PI_BF16 ? launch_commit<__nv_bfloat16>(h, W) : launch_commit<float>(h, W));
+  k_beta_sums<<<(h->m.K + 31) / 32, 1024, 0, h->stream>>>(h->m, W, h->d_shard_R);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(R_out, h->d_shard_R, sizeof(double) * 2 * h->m.K, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->shard_phase = 3;
+  return check_device_err(h);
+}
+
+int ammsb_shard_theta(ammsb_handle* h, const double* R_total) {
+  if (!h || !R_total) return AMMSB_E_ARG;
+  if (h->shard_phase != 3) {
+    h->err = "ammsb_shard_theta follows ammsb_shard_commit";
+    return AMMSB_E_STATE;
+  }
+  CK(cudaSetDevice(h->device));
+  const Buffers& D = h->bufs[h->shard_drawn];
+  CK(cudaMemcpyAsync(h->d_shard_R, R_total, sizeof(double) * 2 * h->m.K, cudaMemcpyHostToDevice, h->stream));
+  k_theta_given<<<(h->m.K + 31) / 32, 1024, 0, h->stream>>>(h->m, D, h->d_shard_R);
+  CK(cudaGetLastError());
+  h->last = h->shard_drawn;
+  h->slot = (h->shard_drawn + 1) % kRing;
+  h->step_count += 1;
+  h->shard_phase = 0;
+  h->shard_drawn = -1;
+  h->ahead = 0;
+  const uint32_t s = (uint32_t)h->step_count;
+  CK(cudaMemcpyAsync(&h->gc->next_step, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+  return check_device_err(h);
+}
 
 int ammsb_get_counters(ammsb_handle* h, uint64_t* edge_evals, uint64_t* iterations) {
   if (!h) return AMMSB_E_ARG;

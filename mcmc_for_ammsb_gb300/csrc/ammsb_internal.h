@@ -31,10 +31,6 @@ struct ammsb_handle {
   cudaStream_t stream = nullptr;  // the handle's stream: updates, perplexity, copies
   cudaStream_t side = nullptr;    // draws of the next iteration, overlapped with the update
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  // the few-node update_phi variant runs beside the many-node one (only one
-  // of them has work in an iteration), so the idle launch is off the path
-  cudaStream_t phi_aux = nullptr;
-  cudaEvent_t ev_phi_fork = nullptr, ev_phi_join = nullptr;
   Model m{};
   DevGraph g{};
   Buffers b{};        // shared state pointers (bufs[s] add the minibatch buffers)
@@ -88,6 +84,12 @@ struct ammsb_handle {
   };
   std::vector<Pending> pending;  // timed launches whose events are not read yet
   uint64_t evals_read = 0;       // edge evaluations counted into the timers' ticks
+  // a sharded iteration in progress (ammsb_shard_*): the drawn buffer set
+  // and the device arrays of its phases
+  int shard_drawn = -1;
+  int shard_phase = 0;  // 1 drawn, 2 owned rows updated, 3 committed
+  int32_t* d_shard_idx = nullptr;  // max(max_nodes, max_edges) slot / edge indices
+  double* d_shard_R = nullptr;     // K x 2 beta-gradient sums
   std::string err;
 };
 

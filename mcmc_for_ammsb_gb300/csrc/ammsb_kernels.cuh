@@ -999,20 +999,48 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
       R1[q * 4 + e] = 0.f;
       bt[q * 4 + e] = (k < K) ? b.beta[k] : 0.f;
     }
-  for (int ed = bb * 4 + warp; ed < n_edges; ed += m.nbb * 4) {
-    const float* pa = b.stage + (int64_t)b.ea[ed] * Kp;
-    const float* pb = b.stage + (int64_t)b.eb[ed] * Kp;
-    const bool y = b.ey[ed] != 0;
+  // The warp's edges ed, ed + stride, ...: each edge's endpoints and label
+  // are loaded one edge ahead, and the first endpoint's row stays in
+  // registers while it repeats -- in the star minibatches of the stratified
+  // strategies every edge starts at the same node, so only the partner's row
+  // is read per edge.
+  const int stride = m.nbb * 4;
+  int ed = bb * 4 + warp;
+  int32_t next_a = 0, next_b = 0;
+  uint8_t next_y = 0;
+  if (ed < n_edges) {
+    next_a = b.ea[ed];
+    next_b = b.eb[ed];
+    next_y = b.ey[ed];
+  }
+  int32_t row_a = -1;
+  float4 xa_row[KQ];
+  for (; ed < n_edges; ed += stride) {
+    const int32_t ia = next_a, ib = next_b;
+    const bool y = next_y != 0;
+    if (ed + stride < n_edges) {
+      next_a = b.ea[ed + stride];
+      next_b = b.eb[ed + stride];
+      next_y = b.ey[ed + stride];
+    }
+    if (ia != row_a) {  // the same for every lane: one edge per warp
+      const float* pa = b.stage + (int64_t)ia * Kp;
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) {
+        const int k0 = q * 128 + lane * 4;
+        xa_row[q] = (k0 < Kp) ? *reinterpret_cast<const float4*>(pa + k0) : make_float4(0, 0, 0, 0);
+      }
+      row_a = ia;
+    }
+    const float* pb = b.stage + (int64_t)ib * Kp;
     float f[KQ * 4];
     float fsum = 0.f, psum = 0.f;
 #pragma unroll
     for (int q = 0; q < KQ; ++q) {
       const int k0 = q * 128 + lane * 4;
-      float4 xa = make_float4(0, 0, 0, 0), xb = make_float4(0, 0, 0, 0);
-      if (k0 < Kp) {
-        xa = *reinterpret_cast<const float4*>(pa + k0);
-        xb = *reinterpret_cast<const float4*>(pb + k0);
-      }
+      const float4 xa = xa_row[q];
+      float4 xb = make_float4(0, 0, 0, 0);
+      if (k0 < Kp) xb = *reinterpret_cast<const float4*>(pb + k0);
       f[q * 4 + 0] = xa.x * xb.x;
       f[q * 4 + 1] = xa.y * xb.y;
       f[q * 4 + 2] = xa.z * xb.z;
@@ -1069,7 +1097,12 @@ __global__ void __launch_bounds__(128) k_commit_beta_chains(const ChainArgs* __r
 //   G_k0 = beta R1 (0 - 1/ts) + (1-beta) R0 (1/theta_k0 - 1/ts)
 //   G_k1 = beta R1 (1/theta_k1 - 1/ts) + (1-beta) R0 (0 - 1/ts)
 // ---------------------------------------------------------------------------
-static __device__ __forceinline__ void theta_body(const Model& m, const Buffers& b) {
+// With R_given the sums are read from it (R0_k, R1_k at 2k, 2k + 1) instead
+// of being formed from the partials; with R_out the sums are written there
+// and no step is taken (the phases of a sharded iteration).
+static __device__ __forceinline__ void theta_body(const Model& m, const Buffers& b,
+                                                  const double* R_given = nullptr,
+                                                  double* R_out = nullptr) {
   // 32 consecutive k per CTA; warp w sums the partials of the active beta
   // blocks w, w+32, ... in FP32 with Kahan compensation, then warp 0 adds
   // the 32 warp sums in fixed order (deterministic) and takes the FP64 step.
@@ -1086,10 +1119,13 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
   const bool kin = k < m.K;
   const double th0 = kin ? b.theta[2 * k] : 1.0, th1 = kin ? b.theta[2 * k + 1] : 1.0;
   const double bt = kin ? (double)b.beta[k] : 0.0;
+  if (R_given) {
+    if (warp != 0 || !kin) return;
+  }
   // the warp's partials (blocks warp, warp + 32, ...) loaded eight at a
   // time, each eight together, then added in block order
   float r0 = 0.f, c0 = 0.f, r1 = 0.f, c1 = 0.f;
-  for (int base = warp; base < active; base += 32 * 8) {
+  for (int base = warp; base < (R_given ? 0 : active); base += 32 * 8) {
     float p0v[8], p1v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -1111,24 +1147,36 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
       }
     }
   }
-  s_r0[warp][lane] = r0;
-  s_c0[warp][lane] = c0;
-  s_r1[warp][lane] = r1;
-  s_c1[warp][lane] = c1;
-  __syncthreads();
-  if (warp != 0 || k >= m.K) return;
-  float a0 = 0.f, e0 = 0.f, a1 = 0.f, e1 = 0.f;  // Kahan over the 32 warp sums
+  double R0, R1;
+  if (R_given) {
+    R0 = R_given[2 * k];
+    R1 = R_given[2 * k + 1];
+  } else {
+    s_r0[warp][lane] = r0;
+    s_c0[warp][lane] = c0;
+    s_r1[warp][lane] = r1;
+    s_c1[warp][lane] = c1;
+    __syncthreads();
+    if (warp != 0 || k >= m.K) return;
+    float a0 = 0.f, e0 = 0.f, a1 = 0.f, e1 = 0.f;  // Kahan over the 32 warp sums
 #pragma unroll
-  for (int w = 0; w < 32; ++w) {
-    const float y0 = (s_r0[w][lane] - s_c0[w][lane]) - e0;
-    const float y1 = (s_r1[w][lane] - s_c1[w][lane]) - e1;
-    const float t0 = a0 + y0, t1 = a1 + y1;
-    e0 = (t0 - a0) - y0;
-    e1 = (t1 - a1) - y1;
-    a0 = t0;
-    a1 = t1;
+    for (int w = 0; w < 32; ++w) {
+      const float y0 = (s_r0[w][lane] - s_c0[w][lane]) - e0;
+      const float y1 = (s_r1[w][lane] - s_c1[w][lane]) - e1;
+      const float t0 = a0 + y0, t1 = a1 + y1;
+      e0 = (t0 - a0) - y0;
+      e1 = (t1 - a1) - y1;
+      a0 = t0;
+      a1 = t1;
+    }
+    R0 = (double)a0 - (double)e0;
+    R1 = (double)a1 - (double)e1;
   }
-  const double R0 = (double)a0 - (double)e0, R1 = (double)a1 - (double)e1;
+  if (R_out) {
+    R_out[2 * k] = R0;
+    R_out[2 * k + 1] = R1;
+    return;
+  }
   if (k == 0) {  // the iteration's edge evaluations, counted once it is applied
     b.gc->evals += (unsigned long long)b.st->n_nodes * (unsigned long long)m.n_out;
     b.gc->iters += 1ull;
@@ -1154,6 +1202,14 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
   b.beta[k] = (float)(t1 / (t0 + t1));
 }
 static __global__ void __launch_bounds__(1024) k_theta(Model m, Buffers b) { theta_body(m, b); }
+// the per-k sums R0, R1 of the beta partials, without the step
+static __global__ void __launch_bounds__(1024) k_beta_sums(Model m, Buffers b, double* R_out) {
+  theta_body(m, b, nullptr, R_out);
+}
+// the theta step from given sums
+static __global__ void __launch_bounds__(1024) k_theta_given(Model m, Buffers b, const double* R) {
+  theta_body(m, b, R, nullptr);
+}
 static __global__ void __launch_bounds__(1024) k_theta_chains(const ChainArgs* __restrict__ c, int p) {
   const ChainArgs& a = c[blockIdx.y];
   theta_body(a.m, a.b[p]);

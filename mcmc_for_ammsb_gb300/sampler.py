@@ -216,6 +216,39 @@ class MCMCSamplerStochastic:
                     edge_y=ey[:e], nodes=nodes[:n], nbrs=nbrs[:n * n_out].reshape(n, n_out),
                     nbr_y=nby[:n * n_out].reshape(n, n_out))
 
+    # -- one rank's phases of a sharded iteration (sharded.ShardedChain) -----
+    def shard_draw(self):
+        """Draws iteration step_count's minibatch and neighbour sets on the
+        device (ammsb_shard_draw); returns them as last_minibatch() does."""
+        self._check(_native.lib().ammsb_shard_draw(self._h))
+        return self.last_minibatch()
+
+    def shard_update(self, slots):
+        """update_phi of the drawn nodes at `slots` (ascending); returns
+        their new pi rows (len(slots) x K, float32)."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        rows = np.zeros((slots.shape[0], self.K), np.float32)
+        self._check(_native.lib().ammsb_shard_update(
+            self._h, slots.shape[0], slots.ctypes.data_as(_native._I32P),
+            rows.ctypes.data_as(_native._F32P)))
+        return rows
+
+    def shard_commit(self, rows_all, edge_idx):
+        """Commits every drawn node's new pi row (slot order) and returns
+        the beta-gradient sums over the edges at `edge_idx` (K x 2)."""
+        rows_all = np.ascontiguousarray(rows_all, np.float32)
+        edge_idx = np.ascontiguousarray(edge_idx, np.int32)
+        R = np.zeros((self.K, 2), np.float64)
+        self._check(_native.lib().ammsb_shard_commit(
+            self._h, rows_all.ctypes.data_as(_native._F32P), edge_idx.shape[0],
+            edge_idx.ctypes.data_as(_native._I32P), R.ctypes.data_as(_native._F64P)))
+        return R
+
+    def shard_theta(self, R_total):
+        """The theta step from the beta-gradient sums of all ranks."""
+        R_total = np.ascontiguousarray(R_total, np.float64)
+        self._check(_native.lib().ammsb_shard_theta(self._h, R_total.ctypes.data_as(_native._F64P)))
+
     def counters(self):
         """(edge evaluations, iterations) sampled on the device so far."""
         e, i = ctypes.c_uint64(), ctypes.c_uint64()

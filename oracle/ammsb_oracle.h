@@ -159,6 +159,17 @@ void oracle_update_beta_f64(int32_t K, const double *pi, const int32_t *ea,
                             double scale, const double *noise,
                             double *grads_out);
 
+/* The two halves of update_beta: the gradient over the given edges (K x 2,
+ * in edge order) and the theta step from a gradient (sums of the halves
+ * over disjoint edge sets give the whole minibatch's gradient). */
+void oracle_beta_grads_f32(int32_t K, const float *pi, const int32_t *ea,
+                           const int32_t *eb, const uint8_t *ey, int32_t n_edges,
+                           const float *theta, const float *beta, float epsilon,
+                           float *grads);
+void oracle_theta_step_f32(int32_t K, float *theta, float *beta, const float *eta,
+                           float eps_t, float scale, const float *noise,
+                           const float *grads);
+
 /* cal_edge_likelihood (learner.h:100-139) */
 float oracle_edge_likelihood_f32(int32_t K, const float *pa, const float *pb,
                                  int y, const float *beta, float epsilon);

@@ -52,15 +52,16 @@ void SFX(oracle_normalize)(int32_t K, const REAL *phi_i, REAL *pi_i) {
   for (int32_t k = 0; k < K; ++k) pi_i[k] = phi_i[k] / s;
 }
 
-/* MCMCSamplerStochastic::update_beta, mcmc_sampler_stochastic.cc:200-267 */
-void SFX(oracle_update_beta)(int32_t K, const REAL *pi, const int32_t *ea,
-                             const int32_t *eb, const uint8_t *ey,
-                             int32_t n_edges, REAL *theta, REAL *beta,
-                             const REAL *eta, REAL epsilon, REAL eps_t,
-                             REAL scale, const REAL *noise, REAL *grads_out) {
-  REAL *grads = (REAL *)calloc(2 * (size_t)K, sizeof(REAL));
+/* MCMCSamplerStochastic::update_beta, mcmc_sampler_stochastic.cc:200-267,
+ * in its two halves: the gradient summed over the minibatch edges in their
+ * order (cc:212-240; grads K x 2, zeroed first) ... */
+void SFX(oracle_beta_grads)(int32_t K, const REAL *pi, const int32_t *ea,
+                            const int32_t *eb, const uint8_t *ey,
+                            int32_t n_edges, const REAL *theta,
+                            const REAL *beta, REAL epsilon, REAL *grads) {
   REAL *probs = (REAL *)malloc(sizeof(REAL) * (size_t)K);
   REAL *theta_sum = (REAL *)malloc(sizeof(REAL) * (size_t)K);
+  for (int32_t k = 0; k < 2 * K; ++k) grads[k] = R(0.0);
   for (int32_t k = 0; k < K; ++k)
     theta_sum[k] = R(0.0) + theta[2 * k] + theta[2 * k + 1];
   for (int32_t ed = 0; ed < n_edges; ++ed) {
@@ -84,8 +85,15 @@ void SFX(oracle_update_beta)(int32_t K, const REAL *pi, const int32_t *ea,
       grads[2 * k + 1] += f * ((REAL)y / theta[2 * k + 1] - one_over_theta_sum);
     }
   }
-  if (grads_out)
-    for (int32_t k = 0; k < 2 * K; ++k) grads_out[k] = grads[k];
+  free(theta_sum);
+  free(probs);
+}
+
+/* ... and the SGRLD step of theta with those gradients, then beta
+ * (cc:244-266) */
+void SFX(oracle_theta_step)(int32_t K, REAL *theta, REAL *beta, const REAL *eta,
+                            REAL eps_t, REAL scale, const REAL *noise,
+                            const REAL *grads) {
   for (int32_t k = 0; k < K; ++k) {
     for (int c = 0; c < 2; ++c) {
       REAL th = theta[2 * k + c];
@@ -101,8 +109,18 @@ void SFX(oracle_update_beta)(int32_t K, const REAL *pi, const int32_t *ea,
     REAL s = R(0.0) + theta[2 * k] + theta[2 * k + 1];
     beta[k] = theta[2 * k + 1] / s;
   }
-  free(theta_sum);
-  free(probs);
+}
+
+void SFX(oracle_update_beta)(int32_t K, const REAL *pi, const int32_t *ea,
+                             const int32_t *eb, const uint8_t *ey,
+                             int32_t n_edges, REAL *theta, REAL *beta,
+                             const REAL *eta, REAL epsilon, REAL eps_t,
+                             REAL scale, const REAL *noise, REAL *grads_out) {
+  REAL *grads = (REAL *)calloc(2 * (size_t)K, sizeof(REAL));
+  SFX(oracle_beta_grads)(K, pi, ea, eb, ey, n_edges, theta, beta, epsilon, grads);
+  if (grads_out)
+    for (int32_t k = 0; k < 2 * K; ++k) grads_out[k] = grads[k];
+  SFX(oracle_theta_step)(K, theta, beta, eta, eps_t, scale, noise, grads);
   free(grads);
 }
 

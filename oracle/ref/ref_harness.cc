@@ -80,6 +80,14 @@ class RefSampler : public mcmc::learning::MCMCSamplerStochastic {
   }
 
   void set_step(uint64_t s) { step_count = s; }
+
+  // a fresh random stream for the draws from here on (learner.cc:47-59
+  // seeds rng_[i] with (seed + 1 + i, seed)); the held-out set and the state
+  // already drawn stay as they are
+  void reseed(unsigned int s) {
+    delete rng_[0];
+    rng_[0] = new mcmc::Random::Random(s + 1, s, false);
+  }
   uint64_t get_step() const { return step_count; }
   float eps_t() { return get_eps_t(); }
 
@@ -247,6 +255,7 @@ void ref_set_state(void* h, const float* phi, const float* theta) {
 }
 
 void ref_set_step(void* h, uint64_t s) { static_cast<RefSampler*>(h)->set_step(s); }
+void ref_reseed(void* h, uint32_t s) { static_cast<RefSampler*>(h)->reseed(s); }
 uint64_t ref_get_step(void* h) { return static_cast<RefSampler*>(h)->get_step(); }
 float ref_eps_t(void* h) { return static_cast<RefSampler*>(h)->eps_t(); }
 

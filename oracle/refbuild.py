@@ -37,6 +37,7 @@ def lib():
         L.ref_get_state.argtypes = [P, P, P, P, P]
         L.ref_set_state.argtypes = [P, P, P]
         L.ref_set_step.argtypes = [P, ctypes.c_uint64]
+        L.ref_reseed.argtypes = [P, ctypes.c_uint32]
         L.ref_get_step.restype = ctypes.c_uint64
         L.ref_get_step.argtypes = [P]
         L.ref_eps_t.restype = ctypes.c_float
@@ -125,6 +126,10 @@ class RefSampler:
 
     def set_step(self, s):
         lib().ref_set_step(self.h, s)
+
+    def reseed(self, s):
+        """A fresh random stream for the draws from here on."""
+        lib().ref_reseed(self.h, s)
 
     @property
     def step(self):

@@ -1,17 +1,23 @@
 """Generates tests/golden/trajectory_ref_small.npz: held-out perplexity
-trajectories of the reference's own run() loop on the small workload.
+trajectories of the reference's own run() loop on the small workload, from
+a known initial state.
 
 The reference's sequential sampler is compiled from its sources
-(oracle/ref/build_ref.py -> oracle/_ref/libammsb_ref.so).  For each seed it
-loads the small workload's graph (N=5,000, written as relativity text and
-read by the reference's own reader, preprocess/relativity.cc:20-200), draws
-its held-out and test sets with its own RNG (network.cc:503-614),
-initialises phi and theta (mcmc_sampler_stochastic.cc:29-79) and runs
-run() (cc:93-183) for 2,000 iterations with K=32, alpha=1/32, eta=(1, 1),
-epsilon=1e-7, a=0.01, b=1024, c=0.55, num-node-sample 32, minibatch
-N/10 and held-out ratio 0.02, printing the held-out perplexity every 100
-steps.  The fixture records, per seed, the held-out and test sets the
-reference drew and the perplexity it printed at steps 1, 101, ..., 1901.
+(oracle/ref/build_ref.py -> oracle/_ref/libammsb_ref.so).  For each initial
+seed s it loads the small workload's graph (N=5,000, written as relativity
+text and read by the reference's own reader, preprocess/relativity.cc
+:20-200) and draws its held-out and test sets with its own RNG
+(network.cc:503-614).  The state is then set to phi ~ Gamma(1, 1), theta ~
+Gamma(1, 1) from the Philox stream of seed s -- the state the GPU sampler's
+init() draws for that seed, so both sides start from the same bits -- and
+run() (mcmc_sampler_stochastic.cc:93-183) takes 2,000 iterations with K=32,
+alpha=1/32, eta=(1, 1), epsilon=1e-7, a=0.01, b=1024, c=0.55,
+num-node-sample 32, minibatch N/10, held-out ratio 0.02, printing the
+held-out perplexity every 100 steps.  This is repeated with STREAMS fresh
+random streams for the draws (the reference's xorshift128+ reseeded after
+the held-out sets are drawn), so the fixture records, per initial seed,
+the held-out and test sets and STREAMS perplexity curves at steps 1, 101,
+..., 1901.
 
 Run:  python tests/golden/make_ref_trajectory.py
 """
@@ -27,22 +33,31 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-SEEDS = (11, 12, 13, 14, 15, 16)
+INIT_SEEDS = (11, 12)
+STREAMS = 6
 ITERS, INTERVAL = 2000, 100
+K = 32
+ARGS = ["--mcmc.K", str(K), "--mcmc.alpha", "0.03125", "--mcmc.epsilon", "1e-7", "--mcmc.a",
+        "0.01", "--mcmc.b", "1024", "--mcmc.c", "0.55", "-n", "32", "--mcmc.held-out-ratio", "0.02",
+        "-i", str(INTERVAL)]
 LINE = re.compile(r"average_count is: (\d+) step count: (\d+) time: \S+ "
                   r"perplexity for hold out set: (\S+)")
 
 
-def run_seed(und, seed):
-    import refbuild
-    r = refbuild.RefSampler(und, ["--mcmc.K", "32", "--mcmc.alpha", "0.03125",
-                                  "--mcmc.epsilon", "1e-7", "--mcmc.a", "0.01", "--mcmc.b", "1024",
-                                  "--mcmc.c", "0.55", "-n", "32", "--mcmc.held-out-ratio", "0.02",
-                                  "--mcmc.seed", str(seed), "-i", str(INTERVAL)])
-    ha, hb, hy = r.held_out()
-    ta, tb, ty = r.test_set()
-    # run() prints to the process's stdout: collect it from the file
-    # descriptor
+def initial_state(seed, N):
+    """phi (N x K) and theta (K x 2), Gamma(1, 1), from the Philox stream of
+    `seed`: the state the GPU sampler's init() draws (chain 0)."""
+    import oracle
+    L = oracle.lib()
+    phi = np.array([[L.oracle_gamma(seed, 0, oracle.P_PHI_INIT, v, k, 1.0, 1.0) for k in range(K)]
+                    for v in range(N)], np.float32)
+    theta = np.array([[L.oracle_gamma(seed, 0, oracle.P_THETA_INIT, 0, 2 * k + c, 1.0, 1.0)
+                       for c in range(2)] for k in range(K)])
+    return phi, theta
+
+
+def run_curve(r):
+    """run() for ITERS iterations; returns (steps, perplexities) it printed."""
     sys.stdout.flush()
     saved = os.dup(1)
     with tempfile.TemporaryFile(mode="w+") as f:
@@ -50,6 +65,7 @@ def run_seed(und, seed):
         try:
             r.run(ITERS, INTERVAL)
         finally:
+            sys.stdout.flush()
             os.dup2(saved, 1)
             os.close(saved)
         f.seek(0)
@@ -60,26 +76,38 @@ def run_seed(und, seed):
         if m:
             steps.append(int(m.group(2)))
             ppx.append(float(m.group(3)))
-    r.close()
-    return dict(ha=ha, hb=hb, hy=hy, ta=ta, tb=tb, ty=ty, steps=np.array(steps),
-                ppx=np.array(ppx))
+    return steps, np.array(ppx)
 
 
 def make():
+    import refbuild
     from ref import build_ref
-    from mcmc_for_ammsb_gb300 import workloads, Network
+    from mcmc_for_ammsb_gb300 import Network, workloads
 
     build_ref.build()
-    gen = workloads.WORKLOADS["small"]["gen"]
-    net = Network.synthetic(**gen)
+    net = Network.synthetic(**workloads.WORKLOADS["small"]["gen"])
     und = net.undirected_edges()
-    out = dict(seeds=np.array(SEEDS), iters=ITERS, interval=INTERVAL, N=net.N)
-    for s in SEEDS:
-        d = run_seed(und, s)
-        assert list(d["steps"]) == list(range(1, ITERS, INTERVAL)), d["steps"]
-        for k, v in d.items():
+    out = dict(init_seeds=np.array(INIT_SEEDS), streams=STREAMS, iters=ITERS, interval=INTERVAL,
+               N=net.N)
+    for s in INIT_SEEDS:
+        phi, theta = initial_state(s, net.N)
+        curves, sets = [], None
+        for t in range(STREAMS):
+            r = refbuild.RefSampler(und, ARGS + ["--mcmc.seed", str(s)])
+            here = r.held_out() + r.test_set()
+            if sets is None:
+                sets = here
+            assert all(np.array_equal(a, b) for a, b in zip(sets, here))
+            r.set_state(phi, theta.astype(np.float32))
+            r.reseed(1000 + 17 * t)
+            steps, ppx = run_curve(r)
+            r.close()
+            assert steps == list(range(1, ITERS, INTERVAL)), steps
+            curves.append(ppx)
+        for k, v in zip(("ha", "hb", "hy", "ta", "tb", "ty"), sets):
             out["s%d_%s" % (s, k)] = v
-        print("seed", s, "perplexity", d["ppx"][[0, 1, 5, -1]])
+        out["s%d_ppx" % s] = np.array(curves)
+        print("seed", s, "mean curve", np.round(np.mean(curves, 0)[[0, 1, 5, -1]], 4))
     path = os.path.join(HERE, "trajectory_ref_small.npz")
     np.savez_compressed(path, **out)
     return path
