@@ -999,6 +999,22 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
       R1[q * 4 + e] = 0.f;
       bt[q * 4 + e] = (k < K) ? b.beta[k] : 0.f;
     }
+#ifdef AMMSB_COMMIT_PLAIN_LOOP
+  for (int ed = bb * 4 + warp; ed < n_edges; ed += m.nbb * 4) {
+    const float* pa = b.stage + (int64_t)b.ea[ed] * Kp;
+    const float* pb = b.stage + (int64_t)b.eb[ed] * Kp;
+    const bool y = b.ey[ed] != 0;
+    float f[KQ * 4];
+    float fsum = 0.f, psum = 0.f;
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int k0 = q * 128 + lane * 4;
+      float4 xa = make_float4(0, 0, 0, 0), xb = make_float4(0, 0, 0, 0);
+      if (k0 < Kp) {
+        xa = *reinterpret_cast<const float4*>(pa + k0);
+        xb = *reinterpret_cast<const float4*>(pb + k0);
+      }
+#else
   // The warp's edges ed, ed + stride, ...: each edge's endpoints and label
   // are loaded one edge ahead, and the first endpoint's row stays in
   // registers while it repeats -- in the star minibatches of the stratified
@@ -1041,6 +1057,7 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
       const float4 xa = xa_row[q];
       float4 xb = make_float4(0, 0, 0, 0);
       if (k0 < Kp) xb = *reinterpret_cast<const float4*>(pb + k0);
+#endif
       f[q * 4 + 0] = xa.x * xb.x;
       f[q * 4 + 1] = xa.y * xb.y;
       f[q * 4 + 2] = xa.z * xb.z;

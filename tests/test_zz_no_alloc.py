@@ -40,7 +40,7 @@ def _call(L, pi_dev, dtype, K, stride, n_rows, beta_dev, epsilon, ha, hb, hy, H,
 # (not a multiple of the 16-byte vector) in a wider row whose padding holds
 # non-zero values, which must not enter the sums; a row stride above 1,024
 # elements (pi as a column slice of a wider matrix)
-ROWS = [(32, 0, 0.0), (1024, 0, 0.0), (20, 12, 7.0), (32, 2016, 3.0)]
+ROWS = [(32, 0, 0.0), (1024, 0, 0.0), (20, 16, 7.0), (32, 2016, 3.0)]
 
 
 @pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
