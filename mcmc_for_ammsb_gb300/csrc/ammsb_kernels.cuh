@@ -999,7 +999,6 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
       R1[q * 4 + e] = 0.f;
       bt[q * 4 + e] = (k < K) ? b.beta[k] : 0.f;
     }
-#ifdef AMMSB_COMMIT_PLAIN_LOOP
   for (int ed = bb * 4 + warp; ed < n_edges; ed += m.nbb * 4) {
     const float* pa = b.stage + (int64_t)b.ea[ed] * Kp;
     const float* pb = b.stage + (int64_t)b.eb[ed] * Kp;
@@ -1014,50 +1013,6 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
         xa = *reinterpret_cast<const float4*>(pa + k0);
         xb = *reinterpret_cast<const float4*>(pb + k0);
       }
-#else
-  // The warp's edges ed, ed + stride, ...: each edge's endpoints and label
-  // are loaded one edge ahead, and the first endpoint's row stays in
-  // registers while it repeats -- in the star minibatches of the stratified
-  // strategies every edge starts at the same node, so only the partner's row
-  // is read per edge.
-  const int stride = m.nbb * 4;
-  int ed = bb * 4 + warp;
-  int32_t next_a = 0, next_b = 0;
-  uint8_t next_y = 0;
-  if (ed < n_edges) {
-    next_a = b.ea[ed];
-    next_b = b.eb[ed];
-    next_y = b.ey[ed];
-  }
-  int32_t row_a = -1;
-  float4 xa_row[KQ];
-  for (; ed < n_edges; ed += stride) {
-    const int32_t ia = next_a, ib = next_b;
-    const bool y = next_y != 0;
-    if (ed + stride < n_edges) {
-      next_a = b.ea[ed + stride];
-      next_b = b.eb[ed + stride];
-      next_y = b.ey[ed + stride];
-    }
-    if (ia != row_a) {  // the same for every lane: one edge per warp
-      const float* pa = b.stage + (int64_t)ia * Kp;
-#pragma unroll
-      for (int q = 0; q < KQ; ++q) {
-        const int k0 = q * 128 + lane * 4;
-        xa_row[q] = (k0 < Kp) ? *reinterpret_cast<const float4*>(pa + k0) : make_float4(0, 0, 0, 0);
-      }
-      row_a = ia;
-    }
-    const float* pb = b.stage + (int64_t)ib * Kp;
-    float f[KQ * 4];
-    float fsum = 0.f, psum = 0.f;
-#pragma unroll
-    for (int q = 0; q < KQ; ++q) {
-      const int k0 = q * 128 + lane * 4;
-      const float4 xa = xa_row[q];
-      float4 xb = make_float4(0, 0, 0, 0);
-      if (k0 < Kp) xb = *reinterpret_cast<const float4*>(pb + k0);
-#endif
       f[q * 4 + 0] = xa.x * xb.x;
       f[q * 4 + 1] = xa.y * xb.y;
       f[q * 4 + 2] = xa.z * xb.z;
@@ -1164,6 +1119,25 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
       }
     }
   }
+  // the parts of the step that do not depend on the sums -- the FP64
+  // divisions and square roots, the normals -- formed by the warp that takes
+  // the step while the other warps' partial loads are in flight
+  double ts_inv = 0.0, d0 = 0.0, d1 = 0.0, sq0 = 0.0, sq1 = 0.0, n0 = 0.0, n1 = 0.0;
+  if (warp == 0 && kin && !R_out) {
+    ts_inv = 1.0 / (th0 + th1);
+    d0 = 1.0 / th0 - ts_inv;
+    d1 = 1.0 / th1 - ts_inv;
+    sq0 = sqrt(eps_t * th0);
+    sq1 = sqrt(eps_t * th1);
+    if (b.fed_theta_noise) {
+      n0 = b.fed_theta_noise[2 * k];
+      n1 = b.fed_theta_noise[2 * k + 1];
+    } else {
+      const Stream rs{m.seed, m.chain};
+      n0 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k);
+      n1 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k + 1);
+    }
+  }
   double R0, R1;
   if (R_given) {
     R0 = R_given[2 * k];
@@ -1198,20 +1172,10 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
     b.gc->evals += (unsigned long long)b.st->n_nodes * (unsigned long long)m.n_out;
     b.gc->iters += 1ull;
   }
-  const double ts_inv = 1.0 / (th0 + th1);
-  const double G0 = bt * R1 * (-ts_inv) + (1.0 - bt) * R0 * (1.0 / th0 - ts_inv);
-  const double G1 = bt * R1 * (1.0 / th1 - ts_inv) + (1.0 - bt) * R0 * (-ts_inv);
-  const Stream rs{m.seed, m.chain};
-  double n0, n1;
-  if (b.fed_theta_noise) {
-    n0 = b.fed_theta_noise[2 * k];
-    n1 = b.fed_theta_noise[2 * k + 1];
-  } else {
-    n0 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k);
-    n1 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k + 1);
-  }
-  double t0 = fabs(th0 + eps_t / 2.0 * ((double)m.eta0 - th0 + scale * G0) + sqrt(eps_t * th0) * n0);
-  double t1 = fabs(th1 + eps_t / 2.0 * ((double)m.eta1 - th1 + scale * G1) + sqrt(eps_t * th1) * n1);
+  const double G0 = bt * R1 * (-ts_inv) + (1.0 - bt) * R0 * d0;
+  const double G1 = bt * R1 * d1 + (1.0 - bt) * R0 * (-ts_inv);
+  double t0 = fabs(th0 + eps_t / 2.0 * ((double)m.eta0 - th0 + scale * G0) + sq0 * n0);
+  double t1 = fabs(th1 + eps_t / 2.0 * ((double)m.eta1 - th1 + scale * G1) + sq1 * n1);
   if (t0 < 1.0e-24) t0 = 1.0e-24;
   if (t1 < 1.0e-24) t1 = 1.0e-24;
   b.theta[2 * k] = t0;
