@@ -1119,25 +1119,6 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
       }
     }
   }
-  // the parts of the step that do not depend on the sums -- the FP64
-  // divisions and square roots, the normals -- formed by the warp that takes
-  // the step while the other warps' partial loads are in flight
-  double ts_inv = 0.0, d0 = 0.0, d1 = 0.0, sq0 = 0.0, sq1 = 0.0, n0 = 0.0, n1 = 0.0;
-  if (warp == 0 && kin && !R_out) {
-    ts_inv = 1.0 / (th0 + th1);
-    d0 = 1.0 / th0 - ts_inv;
-    d1 = 1.0 / th1 - ts_inv;
-    sq0 = sqrt(eps_t * th0);
-    sq1 = sqrt(eps_t * th1);
-    if (b.fed_theta_noise) {
-      n0 = b.fed_theta_noise[2 * k];
-      n1 = b.fed_theta_noise[2 * k + 1];
-    } else {
-      const Stream rs{m.seed, m.chain};
-      n0 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k);
-      n1 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k + 1);
-    }
-  }
   double R0, R1;
   if (R_given) {
     R0 = R_given[2 * k];
@@ -1172,10 +1153,20 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
     b.gc->evals += (unsigned long long)b.st->n_nodes * (unsigned long long)m.n_out;
     b.gc->iters += 1ull;
   }
-  const double G0 = bt * R1 * (-ts_inv) + (1.0 - bt) * R0 * d0;
-  const double G1 = bt * R1 * d1 + (1.0 - bt) * R0 * (-ts_inv);
-  double t0 = fabs(th0 + eps_t / 2.0 * ((double)m.eta0 - th0 + scale * G0) + sq0 * n0);
-  double t1 = fabs(th1 + eps_t / 2.0 * ((double)m.eta1 - th1 + scale * G1) + sq1 * n1);
+  const double ts_inv = 1.0 / (th0 + th1);
+  const double G0 = bt * R1 * (-ts_inv) + (1.0 - bt) * R0 * (1.0 / th0 - ts_inv);
+  const double G1 = bt * R1 * (1.0 / th1 - ts_inv) + (1.0 - bt) * R0 * (-ts_inv);
+  const Stream rs{m.seed, m.chain};
+  double n0, n1;
+  if (b.fed_theta_noise) {
+    n0 = b.fed_theta_noise[2 * k];
+    n1 = b.fed_theta_noise[2 * k + 1];
+  } else {
+    n0 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k);
+    n1 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k + 1);
+  }
+  double t0 = fabs(th0 + eps_t / 2.0 * ((double)m.eta0 - th0 + scale * G0) + sqrt(eps_t * th0) * n0);
+  double t1 = fabs(th1 + eps_t / 2.0 * ((double)m.eta1 - th1 + scale * G1) + sqrt(eps_t * th1) * n1);
   if (t0 < 1.0e-24) t0 = 1.0e-24;
   if (t1 < 1.0e-24) t1 = 1.0e-24;
   b.theta[2 * k] = t0;
