@@ -103,14 +103,17 @@ cudaError_t launch_phi_ring_t(ammsb_handle* h, const Buffers& b, bool configure)
     h->phi_smem_wide = use_wide ? smem_w : 0;
     return cudaSuccess;
   }
+  // the many-node kernel walks the node slots grid-stride: one CTA per slot
+  // unless a smaller grid is asked for
+  const int grid = h->cfg.ring_grid > 0 ? std::min(h->cfg.ring_grid, h->m.max_nodes) : h->m.max_nodes;
   if (use_wide) {
     wide<<<std::min(kRingFewNodes, h->m.max_nodes), kRingSplitWide * 32, smem_w, h->stream>>>(
         h->m, b, 0, kRingFewNodes);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, kRingFewNodes, INT32_MAX);
+    kern<<<grid, kRingSplit * 32, smem, h->stream>>>(h->m, b, kRingFewNodes, INT32_MAX);
   } else {
-    kern<<<h->m.max_nodes, kRingSplit * 32, smem, h->stream>>>(h->m, b, 0, INT32_MAX);
+    kern<<<grid, kRingSplit * 32, smem, h->stream>>>(h->m, b, 0, INT32_MAX);
   }
   return cudaGetLastError();
 }
@@ -420,6 +423,17 @@ void choose_config(ammsb_handle* h) {
   c.ring_stages = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 4 : 3;  // fastest ring depths on GB300
   c.ring_few = 1;
   if (const char* env = std::getenv("AMMSB_PHI_FEW")) c.ring_few = std::atoi(env) != 0;
+  // the many-node ring launch: 16 CTAs per SM (four waves of the four that
+  // fit an SM), each walking its node slots; a link-stratum iteration, which
+  // leaves this launch idle, then starts 2,432 empty CTAs on a GB300 instead
+  // of one per node slot (4,097 at m = 4,096): 0.6% less time per BF16
+  // iteration on the 4M-node workload; fewer CTAs (12 or 14 per SM) were
+  // slower (uneven node counts per CTA)
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess || sms < 1)
+    sms = 152;
+  c.ring_grid = 16 * sms;
+  if (const char* env = std::getenv("AMMSB_PHI_GRID")) c.ring_grid = std::max(0, std::atoi(env));
   if (const char* env = std::getenv("AMMSB_PHI_KERNEL")) {  // "ring" or "regs"
     if (std::strcmp(env, "regs") == 0) c.ring = 0;
   }

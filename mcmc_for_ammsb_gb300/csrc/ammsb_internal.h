@@ -21,6 +21,7 @@ struct KernelCfg {
   int ring;                  // wide rows: the shared-memory ring kernel
   int ring_stages;           // its ring depth
   int ring_few;              // a 16-warp variant takes iterations of few nodes
+  int ring_grid;             // CTAs of the many-node ring launch (0: one per node slot)
   int ppx_lpn, ppx_vpl;      // perplexity
   int kq;                    // commit_beta
 };
