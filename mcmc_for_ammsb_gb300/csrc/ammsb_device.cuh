@@ -18,6 +18,24 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return r;
 }
 
+// Programmatic dependent launch (PTX griddepcontrol, sm_90 and later): a
+// kernel launched with the programmatic stream serialization attribute may
+// start before the kernel ahead of it in the stream has finished, once every
+// CTA of that kernel has called grid_launch_dependents() or exited; it must
+// call grid_dependency_wait() before it reads what that kernel writes, and
+// the wait returns once that kernel has completed and its writes are
+// visible.  Both are no-ops in a kernel launched without the attribute.
+// The iteration's kernels keep three rules, under which each early start is
+// safe by looking at the kernel's own reads: (1) a CTA triggers only after
+// its own wait; (2) every CTA waits before it exits; (3) before its wait a
+// kernel reads only what kernels at least two launches ahead in the stream
+// wrote (or draws joined before the launch ahead).  By (1) and (2) a launch
+// starts only once the kernel two ahead of it has completed.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Error bits of DevState::err (returned to the host as AMMSB_E_*).
 enum : int32_t {
   kErrMinibatchCap = 1,  // minibatch rejection loop hit its cap

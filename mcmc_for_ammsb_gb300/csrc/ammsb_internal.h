@@ -16,12 +16,19 @@ using namespace ammsb;
 
 constexpr int kRing = 4;  // minibatch buffer sets per handle
 
+// Launches of the iteration that may start before the kernel ahead of them
+// has finished (programmatic dependent launch): update_phi after the
+// previous iteration's theta step, the commit after update_phi, the theta
+// step after the commit.
+enum : int { kPdlPhi = 1, kPdlCommit = 2, kPdlTheta = 4 };
+
 struct KernelCfg {
   int lpn, vpl, split, npb;  // update_phi
   int ring;                  // wide rows: the shared-memory ring kernel
   int ring_stages;           // its ring depth
   int ring_few;              // a 16-warp variant takes iterations of few nodes
   int ring_grid;             // CTAs of the many-node ring launch (0: one per node slot)
+  int pdl;                   // programmatic dependent launches: kPdl* bits
   int ppx_lpn, ppx_vpl;      // perplexity
   int kq;                    // commit_beta
 };

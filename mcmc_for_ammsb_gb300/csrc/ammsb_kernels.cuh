@@ -964,6 +964,10 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
     constexpr int EV = TR::kPerVec;
     PiT* pi = reinterpret_cast<PiT*>(b.pi);
     const int nvec = Kp / EV;
+    // the staged rows come from update_phi, the launch ahead of this one,
+    // which also still reads the pi rows written here
+    grid_dependency_wait();
+    grid_launch_dependents();
     for (int slot = blockIdx.x * 4 + warp; slot < n_nodes; slot += ncommit * 4) {
       const int32_t i = b.nodes[slot];
       const float* src = b.stage + (int64_t)slot * Kp;
@@ -988,7 +992,10 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
   __shared__ float s_part[4][2][KQ * 128];
   const int bb = blockIdx.x - ncommit;
   const int n_edges = b.st->n_edges;
-  if (bb >= m.nbb || bb * 4 >= n_edges) return;  // no edges for this block: k_theta skips its partial
+  if (bb >= m.nbb || bb * 4 >= n_edges) {  // no edges for this block: k_theta skips its partial
+    grid_dependency_wait();
+    return;
+  }
   float R0[KQ * 4], R1[KQ * 4], bt[KQ * 4];
 #pragma unroll
   for (int q = 0; q < KQ; ++q)
@@ -999,6 +1006,8 @@ __device__ __forceinline__ void commit_beta_body(const Model& m, const Buffers& 
       R1[q * 4 + e] = 0.f;
       bt[q * 4 + e] = (k < K) ? b.beta[k] : 0.f;
     }
+  grid_dependency_wait();  // the staged rows (update_phi)
+  grid_launch_dependents();
   for (int ed = bb * 4 + warp; ed < n_edges; ed += m.nbb * 4) {
     const float* pa = b.stage + (int64_t)b.ea[ed] * Kp;
     const float* pb = b.stage + (int64_t)b.eb[ed] * Kp;
@@ -1091,6 +1100,8 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
   const bool kin = k < m.K;
   const double th0 = kin ? b.theta[2 * k] : 1.0, th1 = kin ? b.theta[2 * k + 1] : 1.0;
   const double bt = kin ? (double)b.beta[k] : 0.0;
+  grid_dependency_wait();  // the beta partials: k_commit_beta, the launch ahead
+  grid_launch_dependents();
   if (R_given) {
     if (warp != 0 || !kin) return;
   }

@@ -258,6 +258,8 @@ __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffe
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
       const float rS = 1.0f / S;  // pi = phi / S as phi * (1/S): within 1 ulp
+      grid_dependency_wait();  // beta: written by the theta step ahead of this launch
+      grid_launch_dependents();
       si = 0.f;
 #pragma unroll
       for (int v = 0; v < VPL; ++v) {
@@ -304,6 +306,11 @@ __device__ __forceinline__ void update_phi_ring_body(const Model& m, const Buffe
       for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
       if (lane == 0) s_red[warp] = S;
       __syncthreads();
+      // beta, read from here on, is written by the theta step ahead of this
+      // launch; everything read before (node ids, neighbour words and rows,
+      // phi) was complete before that step started
+      grid_dependency_wait();
+      grid_launch_dependents();
       S = 0.f;
 #pragma unroll
       for (int w = 0; w < SPLIT; ++w) S += s_red[w];
@@ -530,8 +537,13 @@ constexpr int ring_min_blocks() { return SPLIT >= 16 ? 1 : 16 / SPLIT; }
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>
 __global__ void __launch_bounds__(SPLIT * 32, ring_min_blocks<SPLIT>())
     k_update_phi_ring(Model m, Buffers b, int n_lo, int n_hi) {
+  // CTAs with no work wait for the kernel ahead before they exit, so that
+  // this launch completes after it
   const int n_nodes = b.st->n_nodes;
-  if (n_nodes <= n_lo || n_nodes > n_hi) return;
+  if (n_nodes <= n_lo || n_nodes > n_hi) {
+    grid_dependency_wait();
+    return;
+  }
   update_phi_ring_body<PiT, VPL, SPLIT, STAGES, FULL>(m, b);
 }
 template <typename PiT, int VPL, int SPLIT, int STAGES, bool FULL>

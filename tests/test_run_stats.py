@@ -113,26 +113,35 @@ def test_convergence_stops_run(small_net, capfd):
     s.close()
 
 
-def test_launch_modes_give_the_same_chain(small_net):
+@pytest.mark.parametrize("K,dtype", [(32, 0), (1024, 1)], ids=["k32-f32", "k1024-bf16"])
+def test_launch_modes_give_the_same_chain(small_net, monkeypatch, K, dtype):
     """The draws depend only on (seed, chain, step), so the chain is the same
     bit for bit whether the iterations run as CUDA graphs or launched one by
-    one, and with the draws made ahead on a second stream or in the loop's
-    order on one stream."""
+    one, with the draws made ahead on a second stream or in the loop's order
+    on one stream, and with or without the early (programmatic dependent)
+    starts of update_phi, the commit and the theta step (AMMSB_PDL, read at
+    create: 0 none, 7 all three; the default starts update_phi and theta
+    early).  K = 1024 runs the ring kernels and their 16-warp variant."""
     import numpy as np
     net, _ = small_net
     out = {}
-    for graph in (1, 0):
-        for pipeline in (1, 0):
-            o = Options(K=32, num_node_sample=32, held_out_ratio=0.02, use_graph=graph,
-                        pipeline=pipeline)
-            s = MCMCSamplerStochastic(o, net).create()
-            s.init()
-            s.step(37)
-            p1 = s.cal_perplexity_held_out()
-            s.step(20)
-            out[graph, pipeline] = (s.phi, s.pi, s.theta, p1, s.step_count)
-            s.close()
-    ref = out[1, 1]
+    for pdl in (None, "0", "7"):
+        for graph in (1, 0):
+            for pipeline in (1, 0):
+                if pdl is None:
+                    monkeypatch.delenv("AMMSB_PDL", raising=False)
+                else:
+                    monkeypatch.setenv("AMMSB_PDL", pdl)
+                o = Options(K=K, num_node_sample=32, held_out_ratio=0.02, use_graph=graph,
+                            pipeline=pipeline, pi_dtype=dtype)
+                s = MCMCSamplerStochastic(o, net).create()
+                s.init()
+                s.step(37)
+                p1 = s.cal_perplexity_held_out()
+                s.step(20)
+                out[pdl, graph, pipeline] = (s.phi, s.pi, s.theta, p1, s.step_count)
+                s.close()
+    ref = out[None, 1, 1]
     for key, got in out.items():
         for a, b in zip(got, ref):
             assert np.array_equal(a, b), key
