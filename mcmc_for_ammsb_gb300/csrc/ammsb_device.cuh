@@ -26,11 +26,13 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // the wait returns once that kernel has completed and its writes are
 // visible.  Both are no-ops in a kernel launched without the attribute.
 // The iteration's kernels keep three rules, under which each early start is
-// safe by looking at the kernel's own reads: (1) a CTA triggers only after
-// its own wait; (2) every CTA waits before it exits; (3) before its wait a
-// kernel reads only what kernels at least two launches ahead in the stream
-// wrote (or draws joined before the launch ahead).  By (1) and (2) a launch
-// starts only once the kernel two ahead of it has completed.
+// safe by looking at the kernel's own reads: (1) no CTA triggers before its
+// own wait (a CTA that exits without waiting counts as triggered); (2) in
+// every launch at least one CTA waits before it exits (every CTA, where the
+// launch has no work); (3) before its wait a kernel reads only what kernels
+// at least two launches ahead in the stream wrote (or draws joined before
+// the launch ahead).  By (1) and (2) a launch completes after the kernel
+// ahead of it, and starts only once the kernel two ahead has completed.
 __device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

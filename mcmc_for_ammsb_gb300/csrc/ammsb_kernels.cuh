@@ -290,9 +290,10 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
   __syncthreads();
   const uint32_t step = s_step;
   const int flag = s_flag;
-  // eps_t is only read by the update kernels: one thread of warp 1 computes
-  // it (FP64 pow) off the sampling critical path
-  if (tid == 32) b.st->eps = eps_schedule(m.a, m.b, m.c, step);
+  // eps_t is only read by the update kernels: the block's last thread
+  // computes it (FP64 pow), as rows and candidates are dealt from thread 0
+  // up and the last warp has the least sampling work
+  if (tid == (int)blockDim.x - 1) b.st->eps = eps_schedule(m.a, m.b, m.c, step);
   int err = 0;
   int rounds = 0;
   if (flag == 0) {
@@ -316,21 +317,30 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
     uint64_t t = 0;
     // the spec scans candidates t = 0, 1, ... until mb are kept, giving up
     // at `cap`; a round examines R >= need of them in parallel and keeps the
-    // first new valid ones, in order, up to mb.  R grows beyond need (up to
-    // one 4096-candidate pass) while the dedup hash stays at most half full,
-    // so small populations with many repeats finish in a round or two.
+    // first new valid ones, in order, up to mb.  R is what the rounds so far
+    // say `need` new ones take (need at first), plus an eighth and 64, while
+    // the dedup hash stays at most half full: a round's cost grows with R
+    // (a first round of up to 4,096 whatever the need took the 100k-node
+    // workload's non-link minibatch from 16 to 44 us), and small populations
+    // with many repeats still finish in two or three rounds.
     const uint64_t cap = 64ull * (uint64_t)mb + 4096ull;
     const int half = (int)((b.hmask + 1u) / 2u);
+    int64_t seen = 0, kept = 0;  // candidates examined and kept so far
     while (!err && count < mb) {
       const int need = mb - count;
       if (t >= cap) {
         err |= kErrMinibatchCap;
         break;
       }
-      const int R = (int)min((uint64_t)max(need, min(half - count, 4096)), cap - t);
-      // pass A: validity and first-occurrence index per value.  Thread tid
-      // owns the G consecutive candidates c0 + G*tid + j of each chunk of
-      // G*blockDim.x; the first exclusion probes of all G are issued together.
+      const int64_t est = seen == 0 ? need : (kept > 0 ? (need * seen + kept - 1) / kept : half);
+      const int want = (int)min(est + est / 8 + 64, (int64_t)half);
+      const int R = (int)min((uint64_t)max(need, min(half - count, want)), cap - t);
+      const int count0 = count;
+      // pass A: validity and first-occurrence index per value, over chunks
+      // of up to G * 1,024 candidates.  Thread tid examines candidates
+      // c0 + tid + 1024 j of its chunk (one each while the chunk has at most
+      // 1,024); the first exclusion probes of its candidates are issued
+      // together.
       constexpr int G = 4;
       const int chunk = G * (int)blockDim.x;
       for (int c0 = 0; c0 < R; c0 += chunk) {
@@ -339,7 +349,7 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
         unsigned long long key[G], xs[G], xk[G];
 #pragma unroll
         for (int j = 0; j < G; ++j) {
-          const int c = c0 + G * tid + j;
+          const int c = c0 + tid + (int)blockDim.x * j;
           live[j] = c < R;
           u[j] = live[j] ? (int32_t)uniform_below(rs.draw_u64(kTagMbCand, 0, step, t + (uint64_t)c),
                                                   (uint64_t)g.n)
@@ -352,7 +362,7 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
         for (int j = 0; j < G; ++j) xk[j] = live[j] ? __ldg(g.excl + xs[j]) : kEmptyKey;
 #pragma unroll
         for (int j = 0; j < G; ++j) {
-          const int c = c0 + G * tid + j;
+          const int c = c0 + tid + (int)blockDim.x * j;
           if (c >= R) continue;
           const bool linked = live[j] && (row_in_smem ? row_contains(s_row, vdeg, u[j])
                                                       : has_edge(g, v, u[j]));
@@ -374,18 +384,21 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
       }
       __syncthreads();
       // pass B: ordered compaction of first occurrences, one block scan per
-      // chunk (thread-local counts of G consecutive candidates); count is
-      // block-uniform, so every thread leaves the loop together at mb
+      // chunk (thread-local counts of its g consecutive candidates, g the
+      // fewest per thread that cover the chunk); count is block-uniform, so
+      // every thread leaves the loop together at mb
       for (int c0 = 0; c0 < R && count < mb; c0 += chunk) {
+        const int n = min(R - c0, chunk);
+        const int gper = (n + (int)blockDim.x - 1) / (int)blockDim.x;
         int32_t u[G];
         bool acc[G];
         int mine = 0;
 #pragma unroll
         for (int j = 0; j < G; ++j) {
-          const int c = c0 + G * tid + j;
+          const int c = c0 + gper * tid + j;
           u[j] = -1;
           acc[j] = false;
-          if (c < R) {
+          if (j < gper && c < c0 + n) {
             u[j] = b.cand[c];
             if (u[j] >= 0) {
               uint32_t slot = hash32((uint32_t)u[j]) & b.hmask;
@@ -420,6 +433,8 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
         count = min(count + total, mb);
       }
       t += (uint64_t)R;
+      seen += R;
+      kept += count - count0;
       ++rounds;
       __syncthreads();
     }
