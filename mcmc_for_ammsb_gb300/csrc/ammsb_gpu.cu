@@ -829,7 +829,9 @@ int ammsb_create(const ammsb_options* opt_in, const ammsb_graph* graph,
   // commit blocks (4 rows each, grid-strided): two per SM, so an iteration
   // of few nodes does not launch a thousand idle blocks
   h->ncommit = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 3) / 4, 152 * 2));
-  h->nbr_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 7) / 8, 152 * 8));
+  // neighbour blocks (8 warps, one node each, grid-strided): a warp more
+  // than the nodes, so the last one, which computes eps_t, has none
+  h->nbr_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((m.max_nodes + 8) / 8, 152 * 8));
   h->m.nbr_set_cap = next_pow2(std::max<int64_t>(64, 2 * (int64_t)m.n_out));
   h->nbr_smem = (size_t)8 * h->m.nbr_set_cap * sizeof(int32_t);
   if (h->nbr_smem > 48 * 1024) {

@@ -290,10 +290,6 @@ static __device__ __forceinline__ void sample_minibatch_body(const Model& m, con
   __syncthreads();
   const uint32_t step = s_step;
   const int flag = s_flag;
-  // eps_t is only read by the update kernels: the block's last thread
-  // computes it (FP64 pow), as rows and candidates are dealt from thread 0
-  // up and the last warp has the least sampling work
-  if (tid == (int)blockDim.x - 1) b.st->eps = eps_schedule(m.a, m.b, m.c, step);
   int err = 0;
   int rounds = 0;
   if (flag == 0) {
@@ -677,6 +673,13 @@ __device__ __forceinline__ void sample_neighbors_body(const Model& m, const DevG
   const uint32_t step = b.st->step;
   const Stream rs{m.seed, m.chain};
   const uint64_t cap = 64ull * (uint64_t)m.n_out + 4096ull;
+  // eps_t of the iteration (get_eps_t, cc:143; read by the update kernels alone): an
+  // FP64 power, computed by the grid's last warp, which the launch leaves
+  // without a node (the grid has a warp more than the nodes) and which no
+  // other warp waits for; in the single-CTA minibatch kernel its latency
+  // delayed every block barrier (2.8 us of each minibatch)
+  if (blockIdx.x == gridDim.x - 1 && warp == WARPS - 1 && lane == 0)
+    b.st->eps = eps_schedule(m.a, m.b, m.c, step);
   for (int slot = blockIdx.x * WARPS + warp; slot < n_nodes; slot += gridDim.x * WARPS) {
     const int32_t i = b.nodes[slot];
     const int64_t ir0 = g.row_ptr[i];
