@@ -458,7 +458,10 @@ void choose_config(ammsb_handle* h) {
     c.lpn = 32;
     c.vpl = next_pow2((nvec + 31) / 32);
   }
-  c.split = (c.lpn == 32) ? (c.vpl >= 2 ? 4 : 2) : 1;
+  // rows narrower than a warp: sub-groups split a node's neighbours until
+  // the node has a warp (K = 32 BF16: 4 lanes x 8 sub-groups), so that a
+  // minibatch of a few hundred nodes still spreads over the SMs
+  c.split = (c.lpn == 32) ? (c.vpl >= 2 ? 4 : 2) : std::min(8, 32 / c.lpn);
   c.ring = (c.lpn == 32) ? 1 : 0;
   c.ring_stages = (h->opt.pi_dtype == AMMSB_PI_BF16) ? 4 : 3;  // fastest ring depths on GB300
   c.ring_few = 1;

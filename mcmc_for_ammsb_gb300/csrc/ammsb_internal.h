@@ -118,7 +118,7 @@ struct ammsb_handle {
   X(1, 1, 1) X(2, 1, 1) X(4, 1, 1) X(8, 1, 1) X(16, 1, 1) X(32, 1, 1) X(32, 1, 2)       \
   X(32, 1, 4) X(32, 2, 1) X(32, 2, 2) X(32, 2, 4) X(32, 4, 1) X(32, 4, 2) X(32, 4, 4)   \
   X(32, 8, 1) X(32, 8, 2) X(32, 8, 4) X(16, 1, 2) X(8, 1, 2) X(8, 1, 4) X(16, 2, 1)     \
-  X(8, 2, 1) X(8, 4, 1) X(4, 2, 1) X(4, 4, 1)
+  X(8, 2, 1) X(8, 4, 1) X(4, 2, 1) X(4, 4, 1) X(4, 1, 8) X(2, 1, 8) X(1, 1, 8)
 
 // Iterations with at most kRingFewNodes nodes (the link stratum) take a
 // kRingSplitWide-warp variant of the ring update_phi kernel.
