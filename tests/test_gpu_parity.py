@@ -341,6 +341,17 @@ def test_fed_step_matches_oracle(small, K, step, dtype):
 
 
 @pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
+@pytest.mark.parametrize("K,nns", [(8, 13), (12, 3), (16, 31)])
+def test_fed_step_narrow_rows_split(small, K, nns, dtype):
+    """Rows narrower than a warp: 1-4 lanes per node and the node's
+    neighbours split over 8 sub-groups (shapes 1x8, 2x8, 4x8), with rows per
+    sub-group uneven (14 and 32 neighbour rows) or fewer rows than
+    sub-groups (4 rows: half the sub-groups have none)."""
+    net, _ = small
+    run_fed_case(net, K, 11, dtype, num_node_sample=nns)
+
+
+@pytest.mark.parametrize("dtype", [_native.PI_F32, _native.PI_BF16])
 def test_fed_step_link_stratum(small, dtype):
     """A link-stratum (y = 1) minibatch through the fed path."""
     net, _ = small
