@@ -19,12 +19,14 @@
 namespace ammsb {
 
 // Upper bound of Model::nbb, the blocks of k_commit_beta that write beta
-// gradient partials (k_theta reads them back, kMaxBetaBlocks / 32 per warp).
+// gradient partials (k_theta reads them back, up to 9 per warp).
 #ifndef AMMSB_MAX_BETA_BLOCKS
 #define AMMSB_MAX_BETA_BLOCKS 256
 #endif
 constexpr int kMaxBetaBlocks = AMMSB_MAX_BETA_BLOCKS;
-static_assert(kMaxBetaBlocks % 256 == 0, "k_theta reads the partials in chunks of 8 per warp");
+// k_theta's 31 summing warps read up to 9 partials each in one pass
+constexpr int kThetaSumWarps = 31, kThetaPerPass = 9;
+static_assert(kMaxBetaBlocks <= kThetaSumWarps * kThetaPerPass, "k_theta reads the partials in one pass");
 
 struct Model {
   int32_t K;      // communities
@@ -1091,6 +1093,33 @@ __global__ void __launch_bounds__(128) k_commit_beta_chains(const ChainArgs* __r
 }
 
 // ---------------------------------------------------------------------------
+// The parts of k's step that do not depend on the sums: 1/(theta0+theta1),
+// the two gradient factors 1/theta_kc - 1/ts, and the two noise terms
+// sqrt(eps theta_kc) n_kc -- three FP64 divisions and two square roots.
+struct ThetaPre {
+  double ts_inv, f0, f1, nz0, nz1;
+};
+static __device__ __forceinline__ ThetaPre theta_pre(const Model& m, const Buffers& b, int k,
+                                                     uint32_t step, double eps_t, double th0,
+                                                     double th1) {
+  ThetaPre p;
+  p.ts_inv = 1.0 / (th0 + th1);
+  p.f0 = 1.0 / th0 - p.ts_inv;
+  p.f1 = 1.0 / th1 - p.ts_inv;
+  const Stream rs{m.seed, m.chain};
+  double n0, n1;
+  if (b.fed_theta_noise) {
+    n0 = b.fed_theta_noise[2 * k];
+    n1 = b.fed_theta_noise[2 * k + 1];
+  } else {
+    n0 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k);
+    n1 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k + 1);
+  }
+  p.nz0 = sqrt(eps_t * th0) * n0;
+  p.nz1 = sqrt(eps_t * th1) * n1;
+  return p;
+}
+
 // k_theta: theta step of update_beta (cc:241-266) in FP64.  With the block
 // sums R0_k, R1_k and beta_k the gradients of cc:236-239 are
 //   G_k0 = beta R1 (0 - 1/ts) + (1-beta) R0 (1/theta_k0 - 1/ts)
@@ -1102,10 +1131,14 @@ __global__ void __launch_bounds__(128) k_commit_beta_chains(const ChainArgs* __r
 static __device__ __forceinline__ void theta_body(const Model& m, const Buffers& b,
                                                   const double* R_given = nullptr,
                                                   double* R_out = nullptr) {
-  // 32 consecutive k per CTA; warp w sums the partials of the active beta
-  // blocks w, w+32, ... in FP32 with Kahan compensation, then warp 0 adds
-  // the 32 warp sums in fixed order (deterministic) and takes the FP64 step.
-  __shared__ float s_r0[32][33], s_c0[32][33], s_r1[32][33], s_c1[32][33];
+  // 32 consecutive k per CTA (lane = k); warps 0-30 sum the partials of the
+  // active beta blocks w, w+31, ... in FP32 with Kahan compensation while
+  // warp 31 forms the FP64 parts of the step that do not need the sums;
+  // then warp 0 adds the 31 warp sums in fixed order (deterministic) and
+  // finishes the step: two FMA chains and one division after the barrier.
+  constexpr int kSumWarps = kThetaSumWarps;
+  __shared__ float s_r0[kSumWarps][33], s_c0[kSumWarps][33], s_r1[kSumWarps][33], s_c1[kSumWarps][33];
+  __shared__ double s_pre[5][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + lane;
   const int Kp = m.Kp;
@@ -1120,48 +1153,60 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
   const double bt = kin ? (double)b.beta[k] : 0.0;
   grid_dependency_wait();  // the beta partials: k_commit_beta, the launch ahead
   grid_launch_dependents();
+  double R0, R1;
+  ThetaPre pre;
   if (R_given) {
     if (warp != 0 || !kin) return;
-  }
-  // the warp's partials (blocks warp, warp + 32, ...) loaded eight at a
-  // time, each eight together, then added in block order
-  float r0 = 0.f, c0 = 0.f, r1 = 0.f, c1 = 0.f;
-  for (int base = warp; base < (R_given ? 0 : active); base += 32 * 8) {
-    float p0v[8], p1v[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int bb = base + 32 * q;
-      const bool on = kin && bb < active;
-      const float* p0 = b.beta_part + (int64_t)bb * 2 * Kp + k;
-      p0v[q] = on ? p0[0] : 0.f;
-      p1v[q] = on ? p0[Kp] : 0.f;
-    }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (base + 32 * q < active) {
-        const float y0 = p0v[q] - c0, y1 = p1v[q] - c1;
-        const float t0 = r0 + y0, t1 = r1 + y1;
-        c0 = (t0 - r0) - y0;
-        c1 = (t1 - r1) - y1;
-        r0 = t0;
-        r1 = t1;
-      }
-    }
-  }
-  double R0, R1;
-  if (R_given) {
     R0 = R_given[2 * k];
     R1 = R_given[2 * k + 1];
+    pre = theta_pre(m, b, k, step, eps_t, th0, th1);
   } else {
-    s_r0[warp][lane] = r0;
-    s_c0[warp][lane] = c0;
-    s_r1[warp][lane] = r1;
-    s_c1[warp][lane] = c1;
+    if (warp == kSumWarps) {
+      if (kin && !R_out) {
+        const ThetaPre q = theta_pre(m, b, k, step, eps_t, th0, th1);
+        s_pre[0][lane] = q.ts_inv;
+        s_pre[1][lane] = q.f0;
+        s_pre[2][lane] = q.f1;
+        s_pre[3][lane] = q.nz0;
+        s_pre[4][lane] = q.nz1;
+      }
+    } else {
+      // the warp's partials (blocks warp, warp + 31, ...) loaded together,
+      // then added in block order
+      float r0 = 0.f, c0 = 0.f, r1 = 0.f, c1 = 0.f;
+      constexpr int P = kThetaPerPass;
+      for (int base = warp; base < active; base += kSumWarps * P) {
+        float p0v[P], p1v[P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          const int bb = base + kSumWarps * q;
+          const bool on = kin && bb < active;
+          const float* p0 = b.beta_part + (int64_t)bb * 2 * Kp + k;
+          p0v[q] = on ? p0[0] : 0.f;
+          p1v[q] = on ? p0[Kp] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          if (base + kSumWarps * q < active) {
+            const float y0 = p0v[q] - c0, y1 = p1v[q] - c1;
+            const float t0 = r0 + y0, t1 = r1 + y1;
+            c0 = (t0 - r0) - y0;
+            c1 = (t1 - r1) - y1;
+            r0 = t0;
+            r1 = t1;
+          }
+        }
+      }
+      s_r0[warp][lane] = r0;
+      s_c0[warp][lane] = c0;
+      s_r1[warp][lane] = r1;
+      s_c1[warp][lane] = c1;
+    }
     __syncthreads();
     if (warp != 0 || k >= m.K) return;
-    float a0 = 0.f, e0 = 0.f, a1 = 0.f, e1 = 0.f;  // Kahan over the 32 warp sums
+    float a0 = 0.f, e0 = 0.f, a1 = 0.f, e1 = 0.f;  // Kahan over the warp sums
 #pragma unroll
-    for (int w = 0; w < 32; ++w) {
+    for (int w = 0; w < kSumWarps; ++w) {
       const float y0 = (s_r0[w][lane] - s_c0[w][lane]) - e0;
       const float y1 = (s_r1[w][lane] - s_c1[w][lane]) - e1;
       const float t0 = a0 + y0, t1 = a1 + y1;
@@ -1172,30 +1217,25 @@ static __device__ __forceinline__ void theta_body(const Model& m, const Buffers&
     }
     R0 = (double)a0 - (double)e0;
     R1 = (double)a1 - (double)e1;
-  }
-  if (R_out) {
-    R_out[2 * k] = R0;
-    R_out[2 * k + 1] = R1;
-    return;
+    if (R_out) {
+      R_out[2 * k] = R0;
+      R_out[2 * k + 1] = R1;
+      return;
+    }
+    pre.ts_inv = s_pre[0][lane];
+    pre.f0 = s_pre[1][lane];
+    pre.f1 = s_pre[2][lane];
+    pre.nz0 = s_pre[3][lane];
+    pre.nz1 = s_pre[4][lane];
   }
   if (k == 0) {  // the iteration's edge evaluations, counted once it is applied
     b.gc->evals += (unsigned long long)b.st->n_nodes * (unsigned long long)m.n_out;
     b.gc->iters += 1ull;
   }
-  const double ts_inv = 1.0 / (th0 + th1);
-  const double G0 = bt * R1 * (-ts_inv) + (1.0 - bt) * R0 * (1.0 / th0 - ts_inv);
-  const double G1 = bt * R1 * (1.0 / th1 - ts_inv) + (1.0 - bt) * R0 * (-ts_inv);
-  const Stream rs{m.seed, m.chain};
-  double n0, n1;
-  if (b.fed_theta_noise) {
-    n0 = b.fed_theta_noise[2 * k];
-    n1 = b.fed_theta_noise[2 * k + 1];
-  } else {
-    n0 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k);
-    n1 = normal_draw(rs, kTagThetaNoise, 0, step, 2ull * k + 1);
-  }
-  double t0 = fabs(th0 + eps_t / 2.0 * ((double)m.eta0 - th0 + scale * G0) + sqrt(eps_t * th0) * n0);
-  double t1 = fabs(th1 + eps_t / 2.0 * ((double)m.eta1 - th1 + scale * G1) + sqrt(eps_t * th1) * n1);
+  const double G0 = bt * R1 * (-pre.ts_inv) + (1.0 - bt) * R0 * pre.f0;
+  const double G1 = bt * R1 * pre.f1 + (1.0 - bt) * R0 * (-pre.ts_inv);
+  double t0 = fabs(th0 + eps_t / 2.0 * ((double)m.eta0 - th0 + scale * G0) + pre.nz0);
+  double t1 = fabs(th1 + eps_t / 2.0 * ((double)m.eta1 - th1 + scale * G1) + pre.nz1);
   if (t0 < 1.0e-24) t0 = 1.0e-24;
   if (t1 < 1.0e-24) t1 = 1.0e-24;
   b.theta[2 * k] = t0;
