@@ -181,12 +181,16 @@ def test_step_random_edge_and_several_sources_against_oracle(small):
         run_fed_case(net, 32, 11, _native.PI_F32, **kw)
 
 
-def test_sampling_small_population_collisions(native_lib):
-    """N small relative to the draws: many duplicate candidates."""
+@pytest.mark.parametrize("m", [30, 60])
+def test_sampling_small_population_collisions(native_lib, m):
+    """N small relative to the draws: many duplicate candidates.  With m = 60
+    of the ~70 valid partners the non-link rounds run until the population
+    is nearly exhausted, each sized from the acceptance rate of the rounds
+    before it."""
     rng = np.random.default_rng(9)
     net = Network.from_edges(80, rng.integers(0, 80, 200), rng.integers(0, 80, 200))
     net.make_held_out(0.1, seed=2)
-    s, opts = make_sampler(net, K=8, num_node_sample=40, mini_batch_size=30, strategy=0)
+    s, opts = make_sampler(net, K=8, num_node_sample=40, mini_batch_size=m, strategy=0)
     s.set_state(*random_state(net.N, 8))
     check_sampling(s, net, opts, steps=8)
     s.close()
