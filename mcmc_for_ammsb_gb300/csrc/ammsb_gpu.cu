@@ -279,7 +279,11 @@ cudaError_t launch_sampling_phase(ammsb_handle* h, const Buffers& b, cudaStream_
 // ev[1 + 3i ..] after each phase of update i on the update stream, then
 // ev[1 + 3n] before the first draws and ev[2 + 3n + 2i ..] after each of
 // draws i on the draws' stream.
-cudaError_t launch_pipelined(ammsb_handle* h, int s, int n, const cudaEvent_t* ev = nullptr) {
+// `first_pdl`: the previous pair's theta step is the kernel ahead of the
+// first update (a long graph of several pairs), which may then start early
+// too.
+cudaError_t launch_pipelined(ammsb_handle* h, int s, int n, const cudaEvent_t* ev = nullptr,
+                             bool first_pdl = false) {
   cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
   if (e != cudaSuccess) return e;
   if ((e = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess) return e;
@@ -288,7 +292,7 @@ cudaError_t launch_pipelined(ammsb_handle* h, int s, int n, const cudaEvent_t* e
   // draws were joined before this launch)
   for (int i = 0; i < n; ++i)
     if ((e = launch_update_phase(h, h->bufs[(s + i) % kRing], ev ? ev + 1 + 3 * i : nullptr,
-                                 i > 0 && !ev)) != cudaSuccess)
+                                 (i > 0 || first_pdl) && !ev)) != cudaSuccess)
       return e;
   if ((e = mark(ev ? ev[1 + 3 * n] : nullptr, h->side)) != cudaSuccess) return e;
   for (int i = 0; i < n; ++i)
@@ -482,6 +486,8 @@ void choose_config(ammsb_handle* h) {
   // 100k-node one); the commit's early start measured no gain
   c.pdl = kPdlPhi | kPdlTheta;
   if (const char* env = std::getenv("AMMSB_PDL")) c.pdl = std::atoi(env) & (kPdlPhi | kPdlCommit | kPdlTheta);
+  c.graph_pairs = 8;
+  if (const char* env = std::getenv("AMMSB_GRAPH_PAIRS")) c.graph_pairs = std::max(1, std::min(64, std::atoi(env)));
   if (const char* env = std::getenv("AMMSB_PHI_KERNEL")) {  // "ring" or "regs"
     if (std::strcmp(env, "regs") == 0) c.ring = 0;
   }
@@ -541,7 +547,7 @@ const char* ammsb_last_error(const ammsb_handle* h) { return h ? h->err.c_str() 
 void ammsb_destroy(ammsb_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
-  for (auto* set : {h->graph1, h->graph2, h->graph1t, h->graph2t})
+  for (auto* set : {h->graph1, h->graph2, h->graph1t, h->graph2t, h->graphL})
     for (int s = 0; s < kRing; ++s)
       if (set[s]) cudaGraphExecDestroy(set[s]);
   if (h->stream) cudaStreamSynchronize(h->stream);
@@ -961,6 +967,32 @@ int ammsb_step(ammsb_handle* h, int64_t n_iters) {
   };
   int64_t left = n_iters;
   while (left > 0) {
+    // long graphs: graph_pairs pipelined pairs per launch, so that every
+    // update but the launch's first follows a theta step inside the graph
+    // (and may start early), with fewer graph launches
+    const int L = h->cfg.graph_pairs;
+    if (L > 1 && h->opt.use_graph && h->opt.pipeline && !h->timing && left >= 2 * (int64_t)L) {
+      const int s = h->slot;
+      cudaGraphExec_t& g = h->graphL[s];
+      if (!g) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int j = 0; j < L && e == cudaSuccess; ++j) e = launch_pipelined(h, (s + 2 * j) % kRing, 2, nullptr, j > 0);
+        cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+          h->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+          return AMMSB_E_CUDA;
+        }
+        CK(cudaGraphInstantiate(&g, graph, cudaGraphInstantiateFlagUseNodePriority));
+        cudaGraphDestroy(graph);
+      }
+      CK(cudaGraphLaunch(g, h->stream));
+      h->last = (s + 2 * L - 1) % kRing;
+      h->slot = (s + 2 * L) % kRing;
+      left -= 2 * L;
+      continue;
+    }
     const int n = left >= 2 ? 2 : 1;
     const int s = h->slot;
     // run()'s timers: the launch records events between the phases; the
@@ -1387,7 +1419,7 @@ int apply_phi_cfg(ammsb_handle* h, const KernelCfg& c) {
       return AMMSB_E_CUDA;
     }
   }
-  for (auto* gs : {h->graph1, h->graph2})  // the captured iterations used the old kernels
+  for (auto* gs : {h->graph1, h->graph2, h->graph1t, h->graph2t, h->graphL})  // the captured iterations used the old kernels
     for (int i = 0; i < kRing; ++i)
       if (gs[i]) {
         cudaGraphExecDestroy(gs[i]);

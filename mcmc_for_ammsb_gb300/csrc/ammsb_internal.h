@@ -29,6 +29,7 @@ struct KernelCfg {
   int ring_few;              // a 16-warp variant takes iterations of few nodes
   int ring_grid;             // CTAs of the many-node ring launch (0: one per node slot)
   int pdl;                   // programmatic dependent launches: kPdl* bits
+  int graph_pairs;           // pairs of iterations per long graph launch (<= 1: none)
   int ppx_lpn, ppx_vpl;      // perplexity
   int kq;                    // commit_beta
 };
@@ -73,6 +74,7 @@ struct ammsb_handle {
   // captured iterations per ring slot: one iteration, and two iterations
   // with the draws of the following two made alongside
   cudaGraphExec_t graph1[kRing] = {}, graph2[kRing] = {};
+  cudaGraphExec_t graphL[kRing] = {};  // cfg.graph_pairs pipelined pairs of iterations in one launch
   // run()'s per-phase timers (mcmc_sampler_stochastic.cc:93-102), printed
   // as PrintStats does (cc:185-198): wall time and ticks per timer
   struct Timer {
