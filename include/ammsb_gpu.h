@@ -131,7 +131,9 @@ int ammsb_set_state(ammsb_handle *h, const float *phi, const double *theta);
 
 /* n_iters iterations of the loop body of run() (cc:131-174): minibatch,
  * neighbour sets, update_phi, pi, update_beta, step_count++.  No
- * perplexity.  Launched as one CUDA graph per iteration when use_graph. */
+ * perplexity.  With use_graph the iterations are launched as CUDA graphs
+ * (up to 16 iterations per launch, the draws of the next ones overlapped);
+ * the chain is the same bit for bit either way. */
 int ammsb_step(ammsb_handle *h, int64_t n_iters);
 
 /* One iteration with every draw supplied by the caller (parity hook):
