@@ -13,6 +13,7 @@
 // its own step counter and Philox key, so a chain advanced in a batch goes
 // through exactly the states it goes through on its own.
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -153,6 +154,8 @@ struct ammsb_batch {
   int nbr_gx = 1;
   size_t mb_smem = 0, nbr_smem = 0;
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  cudaGraphExec_t execL[2] = {nullptr, nullptr};  // graph_iters iterations per launch
+  int graph_iters = 8;
   int parity = 0;
   bool prefetched = false;
   std::vector<uint64_t> expect_step;  // each chain's step_count after the last batch step
@@ -240,8 +243,9 @@ void ammsb_batch_destroy(ammsb_batch* bt) {
   cudaSetDevice(bt->device);
   if (bt->stream) cudaStreamSynchronize(bt->stream);
   if (bt->side) cudaStreamSynchronize(bt->side);
-  for (auto& g : bt->exec)
-    if (g) cudaGraphExecDestroy(g);
+  for (auto* set : {bt->exec, bt->execL})
+    for (int q = 0; q < 2; ++q)
+      if (set[q]) cudaGraphExecDestroy(set[q]);
   for (void* p : bt->allocs) cudaFree(p);
   for (cudaEvent_t ev : {bt->ev_fork, bt->ev_join, bt->ev_done, bt->ev_groups})
     if (ev) cudaEventDestroy(ev);
@@ -283,6 +287,8 @@ int ammsb_batch_create(ammsb_handle* const* handles, int32_t n, ammsb_batch** ou
     bt->h.push_back(h);
   }
   bt->device = handles[0]->device;
+  if (const char* env = std::getenv("AMMSB_BATCH_GRAPH_ITERS"))  // even; 1 = one iteration per launch
+    bt->graph_iters = std::max(1, std::min(64, std::atoi(env) & ~1));
   int prio_lo = 0, prio_hi = 0;  // the draws ahead at the higher priority, as for one chain
   if (cudaSetDevice(bt->device) != cudaSuccess ||
       cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
@@ -443,22 +449,28 @@ int ammsb_batch_step(ammsb_batch* bt, int64_t n_iters) {
     BK(launch_sampling_chains(bt, 0, bt->stream));
     bt->prefetched = true;
   }
-  for (int64_t it = 0; it < n_iters; ++it) {
+  // graph_iters iterations per graph launch while that many are left (an
+  // even count: the launch ends on the parity it started from), then one
+  for (int64_t it = 0; it < n_iters;) {
     const int p = bt->parity;
-    if (!bt->exec[p]) {
+    const int L = (bt->graph_iters > 1 && n_iters - it >= bt->graph_iters) ? bt->graph_iters : 1;
+    cudaGraphExec_t& g = (L > 1) ? bt->execL[p] : bt->exec[p];
+    if (!g) {
       cudaGraph_t graph;
       BK(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
-      cudaError_t e = launch_pipelined_chains(bt, p);
+      cudaError_t e = cudaSuccess;
+      for (int j = 0; j < L && e == cudaSuccess; ++j) e = launch_pipelined_chains(bt, p ^ (j & 1));
       cudaError_t e2 = cudaStreamEndCapture(bt->stream, &graph);
       if (e != cudaSuccess || e2 != cudaSuccess) {
         bt->err = std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
         return AMMSB_E_CUDA;
       }
-      BK(cudaGraphInstantiate(&bt->exec[p], graph, cudaGraphInstantiateFlagUseNodePriority));
+      BK(cudaGraphInstantiate(&g, graph, cudaGraphInstantiateFlagUseNodePriority));
       cudaGraphDestroy(graph);
     }
-    BK(cudaGraphLaunch(bt->exec[p], bt->stream));
-    bt->parity ^= 1;
+    BK(cudaGraphLaunch(g, bt->stream));
+    bt->parity ^= (L & 1);
+    it += L;
   }
   BK(cudaEventRecord(bt->ev_done, bt->stream));
   for (size_t i = 0; i < bt->h.size(); ++i) {
